@@ -1,0 +1,105 @@
+"""The oracle against the reference's own golden values (no GPU).
+
+K-1  python3/aenet/tests/test_ase.py:58      Ti2O4 total energy
+K-2  python3/aenet/tests/test_core.py:29-30  Rc_min / Rc_max of the Ti/O pair
+K-3  unittests/Cu-dimer-forces               81-point Behler dimer scan
+"""
+import numpy as np
+import pytest
+
+from tests.golden import fixtures
+
+
+@pytest.fixture(scope="module")
+def k1():
+    return fixtures.load("k1_ti2o4.npz")
+
+
+@pytest.fixture(scope="module")
+def k3():
+    return fixtures.load("k3_cu_dimer.npz")
+
+
+def _types(npz, symbols):
+    names = [str(t) for t in npz["types"]]
+    return np.array([names.index(str(s)) + 1 for s in symbols], dtype=np.int32)
+
+
+def test_k1_ti2o4_energy_legacy_angular(oracle, k1):
+    pots = fixtures.potentials(k1)
+    oracle.load(["Ti", "O"], pots, angular="legacy")
+    types = _types(k1, k1["symbols"])
+    ec, et, F, Ea = oracle.structure(k1["cell"], k1["positions"], types)
+    # test_ase.py:58 uses assertAlmostEqual (7 places); the restatement is
+    # exact to the 12 printed digits.
+    assert abs(et - float(k1["E_total"])) < 1e-9
+    assert abs(Ea.sum() - et) < 1e-9
+    # forces sum to zero (translation invariance)
+    assert np.abs(F.sum(axis=0)).max() < 1e-10
+
+
+def test_k1_forces_match_central_differences(oracle, k1):
+    """test_ase.py:62-86: forces vs central differences (d = 0.01)."""
+    pots = fixtures.potentials(k1)
+    oracle.load(["Ti", "O"], pots, angular="legacy")
+    types = _types(k1, k1["symbols"])
+    pos = np.array(k1["positions"])
+    _, _, F, _ = oracle.structure(k1["cell"], pos, types)
+    d = 0.01
+    for ia in range(len(pos)):
+        for c in range(3):
+            p1 = pos.copy(); p1[ia, c] -= d
+            p2 = pos.copy(); p2[ia, c] += d
+            e1 = oracle.structure(k1["cell"], p1, types, forces=False)[1]
+            e2 = oracle.structure(k1["cell"], p2, types, forces=False)[1]
+            assert abs(F[ia, c] + (e2 - e1) / (2 * d)) < 5e-3
+
+
+def test_k2_cutoff_range(oracle, k1):
+    oracle.load(["Ti", "O"], fixtures.potentials(k1))
+    assert oracle.Rc_min == float(k1["Rc_min"])
+    assert oracle.Rc_max == float(k1["Rc_max"])
+
+
+def test_k3_cu_dimer_scan(oracle, k3):
+    types = [str(t) for t in k3["types"]]
+    oracle.load(types, fixtures.potentials(k3))
+    cu = types.index("Cu") + 1
+    for x, F, ec, et in zip(k3["positions"], k3["forces"], k3["E_coh"], k3["E_total"]):
+        ecm, etm, Fm, _ = oracle.structure(None, x, [cu, cu], pbc=False)
+        assert abs(ecm - ec) <= 5.1e-9       # printed with F20.8
+        assert abs(etm - et) <= 5.1e-9
+        assert np.abs(Fm - F).max() <= 5.1e-7  # printed with F12.6
+
+
+def test_k3_cell_list_as_written_misses_far_dimer_partner(oracle, k3):
+    """The linked-cell search of lclist.f90 as written misses the partner of
+    a dimer beyond ~4.6 A in the thin isolated bounding box, so the current
+    reference source would not reproduce its own 2013 outputs there; the
+    complete candidate mode does."""
+    types = [str(t) for t in k3["types"]]
+    oracle.load(types, fixtures.potentials(k3))
+    cu = types.index("Cu") + 1
+    x = k3["positions"][32]            # 5.2 A
+    try:
+        oracle.set_candidates("cells")
+        ec_cells = oracle.structure(None, x, [cu, cu], pbc=False)[0]
+    finally:
+        oracle.set_candidates("complete")
+    ec_full = oracle.structure(None, x, [cu, cu], pbc=False)[0]
+    assert abs(ec_full - k3["E_coh"][32]) < 5.1e-9
+    assert abs(ec_cells - k3["E_coh"][32]) > 1e-3
+
+
+def test_nn_roundtrip_product_writer_oracle_reader(tmp_path, k1, k3):
+    from oracle.nnfile import parse_nn
+    for npz in (k1, k3):
+        pots = fixtures.potentials(npz)
+        paths = fixtures.write_potential_files(pots, str(tmp_path))
+        for t, p in paths.items():
+            back = parse_nn(p)
+            assert back["legacy"] == pots[t]["legacy"]
+            np.testing.assert_array_equal(back["net"]["W"], pots[t]["net"]["W"])
+            np.testing.assert_array_equal(back["stp"]["sfval_avg"], pots[t]["stp"]["sfval_avg"])
+            assert back["stp"]["envtypes"] == list(pots[t]["stp"]["envtypes"])
+            assert back["ts"]["E_atom"].tolist() == list(pots[t]["ts"]["E_atom"])
