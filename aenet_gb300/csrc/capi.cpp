@@ -1,0 +1,1877 @@
+// C-ABI of libaenet_gb300.so: the drop-in libaenet API (include/aenet.h,
+// replacing src/aenet.f90) and the batched GPU extensions
+// (include/aenet_gb300.h).
+//
+// Host state mirrors the reference's module globals (aenet.f90:115-132):
+// one set of potentials per process, loaded from .nn files; when the last
+// potential is loaded the device tables (normalisation, network weights in
+// FP64 and FP32, descriptor parameters) are built once.
+//
+// Evaluation always runs on the GPU.  There is no CPU path: if no CUDA
+// device is usable the entry points return AENET_ERR_CUDA.
+//
+// Compiled with -ffp-contract=off: the reciprocal lattice is computed with
+// the unfused operations of geo_recip_lattice (geometry.f90:491-516) so
+// that lattice coordinates, and therefore neighbour sets, match the
+// reference bit for bit.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/aenet.h"
+#include "../../include/aenet_gb300.h"
+#include "common.h"
+
+#define EXPORT extern "C" __attribute__((visibility("default")))
+
+// ---------------------------------------------------------------------
+// exported data (aenet.f90:101-118)
+// ---------------------------------------------------------------------
+EXPORT int AENET_OK = 0;
+EXPORT int AENET_ERR_INIT = 1;
+EXPORT int AENET_ERR_MALLOC = 2;
+EXPORT int AENET_ERR_IO = 3;
+EXPORT int AENET_ERR_TYPE = 4;
+EXPORT int AENET_TYPELEN = 2;
+EXPORT int AENET_PATHLEN = 1024;
+EXPORT bool AENET_TRUE = true;
+EXPORT bool AENET_FALSE = false;
+EXPORT int aenet_nsf_max = 0;
+EXPORT int aenet_nnb_max = 0;
+EXPORT double aenet_Rc_min = 0.0;
+EXPORT double aenet_Rc_max = 0.0;
+
+namespace {
+
+constexpr double CONST_PI = 3.141592653589793;  // constants.f90
+
+// ---------------------------------------------------------------------
+// .nn potential files (potential.f90:111-157)
+// ---------------------------------------------------------------------
+struct HostNet {
+  int nlayers = 0, nnodes_max = 0, Wsize = 0, nvalues = 0;
+  std::vector<int> nnodes, f_a, iw, iv;
+  std::vector<double> W;
+};
+struct HostSetup {
+  std::string description, atomtype, sftype;
+  std::vector<std::string> envtypes;
+  int nenv = 0, nsf = 0, nsfparam = 0, neval = 0;
+  double Rc_min = 0, Rc_max = 0;
+  std::vector<int> sf, sfenv;
+  std::vector<double> sfparam, vmin, vmax, vavg, vcov;
+  bool legacy = false;
+};
+struct HostTs {
+  std::string file;
+  bool normalized = false;
+  double scale = 1, shift = 0;
+  std::vector<std::string> typeName;
+  std::vector<double> E_atom;
+};
+struct HostPot {
+  bool init = false;
+  HostNet net;
+  HostSetup stp;
+  HostTs ts;
+  double E_scale = 1, E_shift = 0, E_atom = 0;
+  std::string path;
+};
+
+std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r\n");
+  if (a == std::string::npos) return "";
+  size_t b = s.find_last_not_of(" \t\r\n");
+  return s.substr(a, b - a + 1);
+}
+
+std::string lower(std::string s) {
+  for (auto& c : s) c = (char)tolower((unsigned char)c);
+  return s;
+}
+
+// Fortran unformatted sequential records: [int32 n][payload][int32 n]
+bool read_records(const char* path, std::vector<std::string>& recs) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return false;
+  std::string data;
+  char buf[1 << 16];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) data.append(buf, n);
+  fclose(f);
+  size_t i = 0;
+  while (i < data.size()) {
+    if (i + 4 > data.size()) return false;
+    int32_t len;
+    memcpy(&len, data.data() + i, 4);
+    if (len < 0 || i + 8 + (size_t)len > data.size()) return false;
+    int32_t len2;
+    memcpy(&len2, data.data() + i + 4 + len, 4);
+    if (len2 != len) return false;
+    recs.emplace_back(data.data() + i + 4, (size_t)len);
+    i += 8 + (size_t)len;
+  }
+  return true;
+}
+
+template <typename T>
+bool rec_vec(const std::string& r, std::vector<T>& out, size_t count) {
+  if (r.size() != count * sizeof(T)) return false;
+  out.resize(count);
+  if (count) memcpy(out.data(), r.data(), r.size());
+  return true;
+}
+
+template <typename T>
+bool rec_one(const std::string& r, T& out) {
+  if (r.size() != sizeof(T)) return false;
+  memcpy(&out, r.data(), sizeof(T));
+  return true;
+}
+
+std::vector<std::string> split_names(const std::string& r, int n) {
+  std::vector<std::string> v;
+  for (int k = 0; k < n; ++k) v.push_back(trim(r.substr(2 * k, 2)));
+  return v;
+}
+
+// load_Network (feedforward.f90:291-306), load_Setup (sfsetup.f90:585-609),
+// load_TrnSet_info (trainset.f90:432-441).  Returns an AENET status.
+int load_nn(const char* path, const std::vector<std::string>& global_types, HostPot& pot) {
+  std::vector<std::string> r;
+  if (!read_records(path, r)) return 3;
+  if (r.size() != 35 && r.size() != 36) return 3;
+  const bool legacy = r.size() == 35;
+  size_t k = 0;
+  HostNet& net = pot.net;
+  int32_t v;
+  if (!rec_one(r[k++], v)) return 3;
+  net.nlayers = v;
+  if (net.nlayers < 2 || net.nlayers > AE_MAXLAYERS) return 3;
+  if (!rec_one(r[k++], v)) return 3;
+  net.nnodes_max = v;
+  if (!rec_one(r[k++], v)) return 3;
+  net.Wsize = v;
+  if (!rec_one(r[k++], v)) return 3;
+  net.nvalues = v;
+  if (!rec_vec(r[k++], net.nnodes, net.nlayers)) return 3;
+  if (!rec_vec(r[k++], net.f_a, net.nlayers - 1)) return 3;
+  if (!rec_vec(r[k++], net.iw, net.nlayers)) return 3;
+  if (!rec_vec(r[k++], net.iv, net.nlayers)) return 3;
+  if (net.Wsize <= 0 || !rec_vec(r[k++], net.W, net.Wsize)) return 3;
+  // consistency with new_Network's bookkeeping
+  int ws = 0;
+  for (int l = 0; l + 1 < net.nlayers; ++l) ws += (net.nnodes[l] + 1) * net.nnodes[l + 1];
+  if (ws != net.Wsize || net.nnodes[net.nlayers - 1] != 1) return 3;
+  HostSetup& s = pot.stp;
+  s.legacy = legacy;
+  s.description = trim(r[k++]);
+  s.atomtype = trim(r[k++]);
+  if (!rec_one(r[k++], v)) return 3;
+  s.nenv = v;
+  if (s.nenv < 1 || (int)r[k].size() != 2 * s.nenv) return 3;
+  s.envtypes = split_names(r[k++], s.nenv);
+  if (!rec_one(r[k++], s.Rc_min)) return 3;
+  if (!rec_one(r[k++], s.Rc_max)) return 3;
+  s.sftype = trim(r[k++]);
+  if (!rec_one(r[k++], v)) return 3;
+  s.nsf = v;
+  if (!rec_one(r[k++], v)) return 3;
+  s.nsfparam = v;
+  if (s.nsf < 1 || s.nsfparam < 1) return 3;
+  if (!rec_vec(r[k++], s.sf, s.nsf)) return 3;
+  if (!rec_vec(r[k++], s.sfparam, (size_t)s.nsfparam * s.nsf)) return 3;
+  if (r[k].size() % (4 * (size_t)s.nsf) != 0) return 3;
+  {
+    size_t nenvmax = r[k].size() / (4 * (size_t)s.nsf);
+    std::vector<int> raw;
+    rec_vec(r[k++], raw, nenvmax * s.nsf);
+    s.sfenv.assign(2 * (size_t)s.nsf, 0);
+    for (int f = 0; f < s.nsf; ++f)
+      for (size_t q = 0; q < nenvmax && q < 2; ++q) s.sfenv[2 * f + q] = raw[f * nenvmax + q];
+  }
+  if (!rec_one(r[k++], v)) return 3;
+  s.neval = v;
+  if (!rec_vec(r[k++], s.vmin, s.nsf)) return 3;
+  if (!rec_vec(r[k++], s.vmax, s.nsf)) return 3;
+  if (!rec_vec(r[k++], s.vavg, s.nsf)) return 3;
+  if (!legacy) {
+    if (!rec_vec(r[k++], s.vcov, s.nsf)) return 3;
+  }
+  HostTs& ts = pot.ts;
+  ts.file = trim(r[k++]);
+  if (!rec_one(r[k++], v)) return 3;
+  ts.normalized = v != 0;
+  if (!rec_one(r[k++], ts.scale)) return 3;
+  if (!rec_one(r[k++], ts.shift)) return 3;
+  if (!rec_one(r[k++], v)) return 3;
+  int nt = v;
+  if (nt < 1 || (int)r[k].size() != 2 * nt) return 3;
+  ts.typeName = split_names(r[k++], nt);
+  if (!rec_vec(r[k++], ts.E_atom, nt)) return 3;
+  // potential.f90:145-151
+  pot.E_scale = 1.0 / ts.scale;
+  pot.E_shift = ts.shift;
+  int it = -1;
+  for (int q = 0; q < nt; ++q)
+    if (ts.typeName[q] == s.atomtype) {
+      it = q;
+      break;
+    }
+  if (it < 0) return 3;
+  pot.E_atom = ts.E_atom[it];
+  pot.path = path;
+  (void)global_types;
+  pot.init = true;
+  return 0;
+}
+
+// ---------------------------------------------------------------------
+// global state
+// ---------------------------------------------------------------------
+struct DevBlob {
+  void* p = nullptr;
+  ~DevBlob() {
+    if (p) cudaFree(p);
+  }
+};
+
+struct State {
+  bool init = false, loaded = false;
+  int ntypes = 0;
+  std::vector<std::string> types;
+  std::vector<HostPot> pots;
+  int angular_legacy = 0;
+  int cell_div = 2;
+  // device tables
+  bool dev_ready = false;
+  PotDevice pd{};
+  std::unique_ptr<DevBlob> blob;
+  std::vector<std::vector<unsigned char>> behler_host;
+  // stand-alone Chebyshev basis (aenet_sfb_*)
+  bool sfb_init = false;
+  int sfb_ntypes = 0, sfb_rorder = 0, sfb_aorder = 0;
+  double sfb_rRc = 0, sfb_aRc = 0;
+  PotDevice sfb_pd{};
+  std::unique_ptr<DevBlob> sfb_blob;
+  // neighbour list API (aenet_nbl_*)
+  bool nbl_init = false;
+  int nbl_natoms = 0;
+  std::vector<int> nbl_cnt, nbl_jt, nbl_img;
+  std::vector<double> nbl_vec, nbl_cart, nbl_s;
+  std::vector<int> nbl_types;
+  int nbl_cap = 0;
+  double nbl_L[9];
+  int nbl_pbc = 1;
+};
+
+State g;
+std::mutex g_mu;
+
+int cuda_ok() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return 0;
+  return 1;
+}
+
+// typespin of new_SFBasis (sfbasis.f90:142-147) for local type index l
+// (1-based) of a basis with num_types species
+float typespin(int num_types, int l) {
+  int s = -num_types / 2;
+  for (int i = 1; i <= num_types; ++i) {
+    if (s == 0 && (num_types % 2) == 0) s = s + 1;
+    if (i == l) return (float)s;
+    s = s + 1;
+  }
+  return 0.f;
+}
+
+int local_type(const HostSetup& s, const std::string& name) {
+  for (int j = 0; j < s.nenv; ++j)
+    if (s.envtypes[j] == name) return j + 1;
+  return 0;
+}
+
+// lcl_nmax_nbdist (lclist.f90:229-245)
+int nmax_nbdist(double rmin, double rmax) {
+  double V_atom = std::pow(0.5 * rmin, 3);
+  double V_cut = std::pow(rmax + 0.5 * rmin, 3);
+  return (int)std::ceil(V_cut / V_atom * 0.7405);
+}
+
+int odd_pitch(int n) { return (n % 2) ? n : n + 1; }
+
+// Behler tables: registration under the GLOBAL type index and evaluation
+// with the LOCAL (env) index of the central atom's setup, as in
+// setup_symmfunc_Behler2011 (sfsetup.f90:1298) and stp_eval
+// (sfsetup.f90:925-944); the per-species table below is what
+// sf_fingerprint evaluates for a central atom of that species.
+int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out);
+
+int build_device_tables() {
+  if (!cuda_ok()) return AENET_ERR_CUDA;
+  PotDevice pd{};
+  pd.ntypes = g.ntypes;
+  int nsf_max = 0;
+  for (auto& p : g.pots) nsf_max = std::max(nsf_max, p.stp.nsf);
+  if (nsf_max > AE_MAXNSF) return AENET_ERR_INPUT;
+  pd.nsf_max = nsf_max;
+  pd.nsf_pad = (nsf_max + 3) & ~3;
+  pd.Rc_max = aenet_Rc_max;
+  std::string sftype = lower(g.pots[0].stp.sftype);
+  for (auto& p : g.pots)
+    if (lower(p.stp.sftype) != sftype) return AENET_ERR_INPUT;
+  std::vector<double> shift((size_t)g.ntypes * pd.nsf_pad, 0.0), scale(shift.size(), 0.0);
+  std::vector<double> w64;
+  for (int t = 0; t < g.ntypes; ++t) {
+    const HostPot& p = g.pots[t];
+    SpeciesTable& sp = pd.sp[t];
+    sp.nsf = p.stp.nsf;
+    sp.E_scale = p.E_scale;
+    sp.E_shift = p.E_shift;
+    sp.E_atom = p.E_atom;
+    // normalisation (sfsetup.f90:985-1035; legacy 16-record setups use
+    // max(avg - min, max - avg), sfsetup.f90:118-123)
+    for (int k = 0; k < p.stp.nsf; ++k) {
+      double sh = p.stp.vavg[k], s;
+      if (p.stp.legacy) {
+        double a = p.stp.vavg[k] - p.stp.vmin[k], b = p.stp.vmax[k] - p.stp.vavg[k];
+        s = a > b ? a : b;
+      } else {
+        s = std::sqrt(p.stp.vcov[k] - sh * sh);
+      }
+      shift[(size_t)t * pd.nsf_pad + k] = sh;
+      scale[(size_t)t * pd.nsf_pad + k] = (s <= 1.0e-10) ? 0.0 : 1.0 / s;
+    }
+    // network
+    NetTable& nt = sp.net;
+    const HostNet& net = p.net;
+    nt.nlayers = net.nlayers;
+    for (int l = 0; l < net.nlayers; ++l) {
+      nt.nnodes[l] = net.nnodes[l];
+      if (net.nnodes[l] > AE_MAXNODES && l > 0) return AENET_ERR_INPUT;
+    }
+    if (net.nnodes[0] != p.stp.nsf) return AENET_ERR_INPUT;
+    nt.f_a[0] = 0;
+    for (int l = 1; l < net.nlayers; ++l) nt.f_a[l] = net.f_a[l - 1];
+    int iw = 0;
+    for (int l = 0; l + 1 < net.nlayers; ++l) {
+      int nin = net.nnodes[l], nout = net.nnodes[l + 1];
+      int pitch = odd_pitch(nin + 1);
+      nt.pitch[l] = pitch;
+      nt.w_off[l] = (int)w64.size();
+      size_t base = w64.size();
+      w64.resize(base + (size_t)pitch * nout, 0.0);
+      // Fortran W(iw+1 : iw+(nin+1)*nout) is column-major (nout, nin+1)
+      for (int o = 0; o < nout; ++o)
+        for (int c = 0; c <= nin; ++c) w64[base + (size_t)o * pitch + c] = net.W[iw + o + c * nout];
+      iw += (nin + 1) * nout;
+    }
+    // Chebyshev (setup_basis_chebyshev, sfsetup.f90:1162-1179)
+    if (sftype == "chebyshev") {
+      sp.sftype = AE_SF_CHEBYSHEV;
+      ChebTable& ct = sp.cheb;
+      ct.r_Rc = p.stp.sfparam[0];
+      int r_order = (int)std::lround(p.stp.sfparam[1]);
+      ct.a_Rc = p.stp.sfparam[2];
+      int a_order = (int)std::lround(p.stp.sfparam[3]);
+      ct.r_N = r_order + 1;
+      ct.a_N = a_order + 1;
+      if (ct.r_N < 1 || ct.a_N < 1 || ct.r_N > AE_MAXCHEB || ct.a_N > AE_MAXCHEB)
+        return AENET_ERR_INPUT;
+      ct.multi = p.stp.nenv > 1 ? 1 : 0;
+      ct.nsf = (ct.r_N + ct.a_N) * (ct.multi ? 2 : 1);
+      if (ct.nsf != p.stp.nsf) return AENET_ERR_INPUT;
+      ct.r_i1 = 0;
+      ct.a_i1 = ct.r_N;
+      ct.r_i2 = ct.r_N + ct.a_N;
+      ct.a_i2 = 2 * ct.r_N + ct.a_N;
+      ct.angular_legacy = g.angular_legacy;
+      for (int gt = 0; gt < AE_MAXT; ++gt) ct.spin[gt] = 0.f;
+      for (int gt = 0; gt < g.ntypes; ++gt) {
+        int l = local_type(p.stp, g.types[gt]);
+        ct.spin[gt] = l > 0 ? typespin(p.stp.nenv, l) : 0.f;
+      }
+    } else if (sftype == "behler2011") {
+      sp.sftype = AE_SF_BEHLER;
+    } else {
+      return AENET_ERR_INPUT;
+    }
+  }
+  int wtotal = (int)w64.size();
+  for (int t = 0; t < g.ntypes; ++t) pd.sp[t].net.wtotal = wtotal;
+  std::vector<float> w32(w64.begin(), w64.end());
+  std::vector<float> shift2(2 * shift.size()), scale32(scale.size());
+  for (size_t q = 0; q < shift.size(); ++q) {
+    float hi = (float)shift[q];
+    shift2[2 * q] = hi;
+    shift2[2 * q + 1] = (float)(shift[q] - (double)hi);
+    scale32[q] = (float)scale[q];
+  }
+  // Behler tables
+  std::vector<std::vector<unsigned char>> bt;
+  std::vector<double> bt_rc;
+  if (sftype == "behler2011") {
+    int st = build_behler(bt, bt_rc);
+    if (st) return st;
+  }
+  size_t blob_bytes = 0;
+  auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t off_shift = blob_bytes;
+  blob_bytes = align(blob_bytes + shift.size() * 8);
+  size_t off_scale = blob_bytes;
+  blob_bytes = align(blob_bytes + scale.size() * 8);
+  size_t off_w64 = blob_bytes;
+  blob_bytes = align(blob_bytes + w64.size() * 8);
+  size_t off_w32 = blob_bytes;
+  blob_bytes = align(blob_bytes + w32.size() * 4);
+  size_t off_sh2 = blob_bytes;
+  blob_bytes = align(blob_bytes + shift2.size() * 4);
+  size_t off_sc32 = blob_bytes;
+  blob_bytes = align(blob_bytes + scale32.size() * 4);
+  size_t off_beh = blob_bytes;
+  std::vector<size_t> beh_off;
+  for (auto& b : bt) {
+    beh_off.push_back(blob_bytes - off_beh);
+    blob_bytes = align(blob_bytes + b.size());
+  }
+  auto blob = std::make_unique<DevBlob>();
+  if (cudaMalloc(&blob->p, blob_bytes + 256) != cudaSuccess) return AENET_ERR_CUDA;
+  char* base = (char*)blob->p;
+  cudaMemcpy(base + off_shift, shift.data(), shift.size() * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(base + off_scale, scale.data(), scale.size() * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(base + off_w64, w64.data(), w64.size() * 8, cudaMemcpyHostToDevice);
+  cudaMemcpy(base + off_w32, w32.data(), w32.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(base + off_sh2, shift2.data(), shift2.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(base + off_sc32, scale32.data(), scale32.size() * 4, cudaMemcpyHostToDevice);
+  for (size_t q = 0; q < bt.size(); ++q)
+    cudaMemcpy(base + off_beh + beh_off[q], bt[q].data(), bt[q].size(), cudaMemcpyHostToDevice);
+  if (cudaDeviceSynchronize() != cudaSuccess) return AENET_ERR_CUDA;
+  pd.shift = (const double*)(base + off_shift);
+  pd.scale = (const double*)(base + off_scale);
+  pd.w64 = (const double*)(base + off_w64);
+  pd.w32 = (const float*)(base + off_w32);
+  pd.shift2 = (const float2*)(base + off_sh2);
+  pd.scale32 = (const float*)(base + off_sc32);
+  pd.behler_blob = (const unsigned char*)(base + off_beh);
+  for (size_t q = 0; q < bt.size(); ++q) pd.sp[q].behler_off = (int)beh_off[q];
+  g.pd = pd;
+  g.blob = std::move(blob);
+  g.behler_host = bt;
+  g.dev_ready = true;
+  return 0;
+}
+
+int ensure_device() {
+  if (!g.loaded) return AENET_ERR_INIT;
+  if (g.dev_ready) return 0;
+  return build_device_tables();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------
+// Behler tables (defined after the anonymous namespace helpers)
+// ---------------------------------------------------------------------
+namespace {
+int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out) {
+  // sf_init over the global types (sfsetup.f90:800-808, symmfunc.f90:91-140)
+  const int nt = g.ntypes;
+  int nGmax = 0;
+  for (auto& p : g.pots) nGmax = std::max(nGmax, p.stp.nsf);
+  // registered functions: by (type1 global, pair/triple of LOCAL env
+  // indices of that potential's setup), in registration order, per kind
+  struct Fn {
+    int kind;
+    double Rc, p1, p2, p3;
+  };
+  // idx2/idx3 of symmfunc.f90:105-120 over nt types
+  auto idx2 = [&](int i, int j) { return (i - 1) * nt + j; };  // 1-based pair id
+  std::vector<int> idx3((size_t)(nt + 1) * (nt + 1) * (nt + 1), 0);
+  int n3 = 0;
+  for (int i = 1; i <= nt; ++i)
+    for (int j = 1; j <= nt; ++j) {
+      idx3[((size_t)i * (nt + 1) + j) * (nt + 1) + j] = ++n3;
+      for (int k = j + 1; k <= nt; ++k) {
+        ++n3;
+        idx3[((size_t)i * (nt + 1) + j) * (nt + 1) + k] = n3;
+        idx3[((size_t)i * (nt + 1) + k) * (nt + 1) + j] = n3;
+      }
+    }
+  auto IDX3 = [&](int i, int j, int k) { return idx3[((size_t)i * (nt + 1) + j) * (nt + 1) + k]; };
+  int npairs = nt * nt;
+  std::vector<std::vector<std::vector<Fn>>> rad(npairs + 1, std::vector<std::vector<Fn>>(6));
+  std::vector<std::vector<std::vector<Fn>>> ang(n3 + 1, std::vector<std::vector<Fn>>(6));
+  std::vector<int> nG_type(nt + 1, 0);
+  for (int t = 1; t <= nt; ++t) {
+    const HostSetup& s = g.pots[t - 1].stp;
+    for (int f = 0; f < s.nsf; ++f) {
+      int kind = s.sf[f];
+      const double* p = &s.sfparam[(size_t)f * s.nsfparam];
+      int t2 = s.sfenv[2 * f], t3 = s.sfenv[2 * f + 1];
+      double P[4] = {0, 0, 0, 0};
+      for (int q = 0; q < std::min(4, s.nsfparam); ++q) P[q] = p[q];
+      if (kind >= 1 && kind <= 3) {
+        if (t2 < 1 || t2 > nt) return AENET_ERR_INPUT;
+        auto& L = rad[idx2(t, t2)][kind];
+        if ((int)L.size() >= nGmax) return AENET_ERR_INPUT;
+        Fn fn{kind, P[0], 0, 0, 0};
+        if (kind == 2) { fn.p1 = P[1]; fn.p2 = P[2]; }
+        if (kind == 3) { fn.p1 = P[1]; }
+        L.push_back(fn);
+      } else if (kind == 4 || kind == 5) {
+        if (t2 < 1 || t2 > nt || t3 < 1 || t3 > nt) return AENET_ERR_INPUT;
+        auto& L = ang[IDX3(t, t2, t3)][kind];
+        if ((int)L.size() >= nGmax) return AENET_ERR_INPUT;
+        // sf_pG4: Rc, lambda, zeta, eta
+        L.push_back(Fn{kind, P[0], P[1], P[2], P[3]});
+      } else {
+        return AENET_ERR_INPUT;
+      }
+      nG_type[t] += 1;
+    }
+  }
+  // per central GLOBAL species: the table evaluated with type1 = ltype of
+  // the central species in its own setup, neighbour species mapped through
+  // the same setup's ltype.
+  out.clear();
+  rc_max_out.clear();
+  for (int c = 0; c < nt; ++c) {
+    const HostSetup& s = g.pots[c].stp;
+    int type1 = local_type(s, g.types[c]);
+    if (type1 < 1 || type1 > nt) return AENET_ERR_INPUT;
+    if (s.nsf < nG_type[type1]) return AENET_ERR_INPUT;
+    // feature offsets, sf_build_index (symmfunc.f90:284-305)
+    std::vector<int> iG02(npairs + 1, 0), iG03(n3 + 1, 0);
+    {
+      int i = 0;
+      for (int t2 = 1; t2 <= nt; ++t2) {
+        int pij = idx2(type1, t2);
+        iG02[pij] = i;
+        for (int kd = 1; kd <= 5; ++kd) i += (int)rad[pij][kd].size();
+        for (int t3 = t2; t3 <= nt; ++t3) {
+          int tijk = IDX3(type1, t2, t3);
+          iG03[tijk] = i;
+          for (int kd = 1; kd <= 5; ++kd) i += (int)ang[tijk][kd].size();
+        }
+      }
+    }
+    std::vector<BehlerFn> fns;
+    BehlerTable hdr{};
+    hdr.nsf = s.nsf;
+    double rcm = 0;
+    // radial functions for each GLOBAL neighbour species gj
+    for (int gj = 0; gj <= nt; ++gj) {
+      hdr.rad_off[gj] = (int)fns.size();
+      if (gj == nt) break;
+      int lj = local_type(s, g.types[gj]);
+      if (lj < 1 || lj > nt) continue;
+      int pij = idx2(type1, lj);
+      int iG = iG02[pij];
+      for (int kd = 1; kd <= 3; ++kd)
+        for (auto& f : rad[pij][kd]) {
+          BehlerFn b{f.Rc, f.p1, f.p2, f.p3, kd, iG++};
+          rcm = std::max(rcm, f.Rc);
+          fns.push_back(b);
+        }
+    }
+    for (int gj = 0; gj < nt; ++gj)
+      for (int gk = 0; gk < nt; ++gk) {
+        hdr.ang_off[gj * nt + gk] = (int)fns.size();
+        int lj = local_type(s, g.types[gj]), lk = local_type(s, g.types[gk]);
+        if (lj < 1 || lj > nt || lk < 1 || lk > nt) continue;
+        int tijk = IDX3(type1, lj, lk);
+        int iG = iG03[tijk];
+        for (int kd = 4; kd <= 5; ++kd)
+          for (auto& f : ang[tijk][kd]) {
+            BehlerFn b{f.Rc, f.p1, f.p2, f.p3, kd, iG++};
+            rcm = std::max(rcm, f.Rc);
+            fns.push_back(b);
+          }
+      }
+    hdr.ang_off[nt * nt] = (int)fns.size();
+    hdr.nfn = (int)fns.size();
+    hdr.rc_max = rcm;
+    size_t bytes = sizeof(BehlerTable) + sizeof(BehlerFn) * (fns.size() + 1);
+    std::vector<unsigned char> buf(bytes, 0);
+    memcpy(buf.data(), &hdr, sizeof(BehlerTable));
+    BehlerTable* bt = reinterpret_cast<BehlerTable*>(buf.data());
+    if (!fns.empty()) memcpy(bt->fn, fns.data(), sizeof(BehlerFn) * fns.size());
+    out.push_back(std::move(buf));
+    rc_max_out.push_back(rcm);
+  }
+  return 0;
+}
+}  // namespace
+
+// ---------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------
+struct aenet_gpu_plan {
+  int nstruc = 0, natoms = 0, fp64 = 1;
+  bool keep_images = false;
+  std::vector<StructGeom> geom_h;
+  std::vector<int> natoms_h;
+  std::vector<int> pbc_h;
+  const PotDevice* pd = nullptr;   // tables used by this plan
+  int cell_div = 2;
+  double rc = 0;
+  // device memory
+  void* mem = nullptr;
+  size_t mem_bytes = 0;
+  StructGeom* geom_d = nullptr;
+  int* atom_struct = nullptr;
+  int* types0 = nullptr;
+  double* s_wrap = nullptr;
+  double* r_wrap = nullptr;
+  float4* r_f32 = nullptr;
+  int* cell_of = nullptr;
+  int* cell_count = nullptr;
+  int* cell_atoms = nullptr;
+  int ncells = 0, nslots = 0;
+  int cap = 0;
+  int* nb_cnt = nullptr;
+  int* nb_jt = nullptr;
+  void* nb_vec = nullptr;
+  int* nb_img = nullptr;
+  void* G = nullptr;
+  void* dEdG = nullptr;
+  double* E_atom = nullptr;
+  void* Facc = nullptr;
+  double* E_struct = nullptr;
+  double* virial = nullptr;
+  unsigned* status = nullptr;
+  ~aenet_gpu_plan() {
+    if (mem) cudaFree(mem);
+  }
+};
+
+namespace {
+// One cached plan (with its I/O staging buffers) for the host-buffer entry
+// points: a call with the same batch layout (structure sizes, lattices,
+// pbc, precision) reuses the device workspace instead of reallocating it.
+struct HostPlanCache {
+  std::unique_ptr<aenet_gpu_plan> plan;
+  std::vector<int> natoms, pbc;
+  std::vector<double> lattices;
+  int precision = -1;
+  bool isolated = false;
+  char* io = nullptr;
+  size_t io_bytes = 0;
+  cudaStream_t stream = nullptr;
+  ~HostPlanCache() {
+    if (io) cudaFree(io);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  void reset() {
+    plan.reset();
+    if (io) cudaFree(io);
+    io = nullptr;
+    io_bytes = 0;
+  }
+};
+HostPlanCache g_cache;
+}  // namespace
+
+namespace {
+
+void cross(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// geometry of one structure
+int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, int natoms,
+              double rc, int cell_div, int frac_mode, const int* force_nc = nullptr) {
+  memset(&G, 0, sizeof(G));
+  G.pbc = pbc;
+  G.frac_mode = frac_mode;
+  const double rcp = rc + 1.0e-3;
+  G.rc2 = rcp * rcp;   // (Rc + EPS)*(Rc + EPS), lclist.f90:572
+  const double w = rcp / cell_div;
+  double ext = rcp;
+  if (pbc) {
+    for (int q = 0; q < 9; ++q) G.L[q] = lat[q];
+    const double* a1 = lat;
+    const double* a2 = lat + 3;
+    const double* a3 = lat + 6;
+    // geo_cell_volume with avec(i,j) = component i of vector j
+    double V = a1[0] * a2[1] * a3[2] + a1[1] * a2[2] * a3[0] + a1[2] * a2[0] * a3[1] -
+               a1[2] * a2[1] * a3[0] - a1[0] * a2[2] * a3[1] - a1[1] * a2[0] * a3[2];
+    if (!(std::fabs(V) > 0.0) || !std::isfinite(V)) return AENET_ERR_INPUT;
+    double b1[3], b2[3], b3[3];
+    cross(a2, a3, b1);
+    cross(a1, a3, b2);
+    cross(a1, a2, b3);
+    for (int c = 0; c < 3; ++c) {
+      if (frac_mode == 0) {
+        G.B[c] = (b1[c] / V) * 2.0 * CONST_PI;
+        G.B[3 + c] = (-b2[c] / V) * 2.0 * CONST_PI;
+        G.B[6 + c] = (b3[c] / V) * 2.0 * CONST_PI;
+      } else {
+        G.B[c] = b1[c] / V;
+        G.B[3 + c] = -b2[c] / V;
+        G.B[6 + c] = b3[c] / V;
+      }
+    }
+    const double* bb[3] = {b1, b2, b3};
+    for (int a = 0; a < 3; ++a) {
+      double bl = std::sqrt(bb[a][0] * bb[a][0] + bb[a][1] * bb[a][1] + bb[a][2] * bb[a][2]);
+      double h = std::fabs(V) / bl;   // height of the cell along axis a
+      int nc = (int)std::floor(h / w);
+      if (nc < 1) nc = 1;
+      if (nc > 1000) nc = 1000;
+      if (force_nc) nc = force_nc[a];
+      G.nc[a] = nc;
+      G.kr[a] = (int)std::ceil(rcp * nc / h * (1.0 + 1e-12));
+      if (G.kr[a] < 1) G.kr[a] = 1;
+      ext += std::sqrt(lat[3 * a] * lat[3 * a] + lat[3 * a + 1] * lat[3 * a + 1] +
+                       lat[3 * a + 2] * lat[3 * a + 2]);
+    }
+  } else {
+    double mn[3] = {0, 0, 0}, mx[3] = {0, 0, 0};
+    for (int i = 0; i < natoms; ++i)
+      for (int c = 0; c < 3; ++c) {
+        double x = coords ? coords[3 * i + c] : 0.0;
+        if (i == 0 || x < mn[c]) mn[c] = x;
+        if (i == 0 || x > mx[c]) mx[c] = x;
+      }
+    for (int c = 0; c < 3; ++c) {
+      G.origin[c] = mn[c] - 0.5 * rcp;
+      G.box[c] = (mx[c] - mn[c]) + rcp;
+      G.L[4 * c] = G.box[c];
+      int nc = (int)std::floor(G.box[c] / w);
+      if (nc < 1) nc = 1;
+      if (nc > 1000) nc = 1000;
+      G.nc[c] = nc;
+      G.kr[c] = (int)std::ceil(rcp * nc / G.box[c] * (1.0 + 1e-12));
+      if (G.kr[c] < 1) G.kr[c] = 1;
+      ext += std::fabs(G.origin[c]) + G.box[c];
+    }
+  }
+  for (int q = 0; q < 9; ++q) G.Lf[q] = (float)G.L[q];
+  // FP32 distances carry an error below ~1e-6 ext per component; the band
+  // is four times the resulting bound on d^2
+  double err = 4.0 * (2.0 * rcp * 4.0e-7 * ext + 1.0e-6 * G.rc2);
+  G.rc2_lo = std::nextafter((float)(G.rc2 - err), 0.0f);
+  G.rc2_hi = std::nextafter((float)(G.rc2 + err), 1e30f);
+  G.natoms = natoms;
+  return 0;
+}
+
+int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices) {
+  const double rc = P->rc;
+  int cell_off = 0, slot_off = 0, atom_off = 0;
+  size_t natoms = 0;
+  double dens_max = 0;
+  for (int s = 0; s < P->nstruc; ++s) {
+    StructGeom& G = P->geom_h[s];
+    const double* c0 = coords0 ? coords0 + 3 * (size_t)atom_off : nullptr;
+    int st = make_geom(G, lattices ? lattices + 9 * (size_t)s : nullptr, P->pbc_h[s], c0,
+                       P->natoms_h[s], rc, P->cell_div, 0);
+    if (st) return st;
+    int nc = G.nc[0] * G.nc[1] * G.nc[2];
+    double expct = (double)P->natoms_h[s] / nc;
+    int cc = (int)std::ceil(3.0 * expct + 16.0);
+    if (cc > P->natoms_h[s]) cc = std::max(1, P->natoms_h[s]);
+    G.cell_cap = cc;
+    G.cell_off = cell_off;
+    G.slot_off = slot_off;
+    G.atom_off = atom_off;
+    cell_off += nc;
+    slot_off += nc * cc;
+    atom_off += P->natoms_h[s];
+    natoms += P->natoms_h[s];
+    double vol;
+    if (G.pbc) {
+      const double* a = G.L;
+      double c[3];
+      cross(a + 3, a + 6, c);
+      vol = std::fabs(a[0] * c[0] + a[1] * c[1] + a[2] * c[2]);
+    } else {
+      vol = G.box[0] * G.box[1] * G.box[2];
+    }
+    double rcp = rc + 1e-3;
+    double nbexp = 4.18879020478639 * rcp * rcp * rcp * P->natoms_h[s] / vol;
+    if (!G.pbc) nbexp = std::min(nbexp, (double)P->natoms_h[s]);
+    dens_max = std::max(dens_max, nbexp);
+  }
+  P->natoms = (int)natoms;
+  P->ncells = cell_off;
+  P->nslots = slot_off;
+  if (P->cap <= 0) {
+    int cap = (int)std::ceil(1.5 * dens_max + 32.0);
+    P->cap = (cap + 31) & ~31;
+  }
+  // layout
+  const int N = P->natoms;
+  const size_t tsz = P->fp64 ? 8 : 4;
+  const size_t nsf_pad = P->pd ? (size_t)P->pd->nsf_pad : 4;
+  const size_t npairs = (size_t)N * P->cap;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = (off + bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  size_t o_geom = take(sizeof(StructGeom) * P->nstruc);
+  size_t o_as = take(4 * (size_t)N);
+  size_t o_t0 = take(4 * (size_t)N);
+  size_t o_s = take(24 * (size_t)N);
+  size_t o_r = take(24 * (size_t)N);
+  size_t o_rf = take(16 * (size_t)N);
+  size_t o_co = take(4 * (size_t)N);
+  size_t o_cc = take(4 * (size_t)P->ncells);
+  size_t o_ca = take(4 * (size_t)P->nslots);
+  size_t o_nc = take(4 * (size_t)N);
+  size_t o_jt = take(4 * npairs);
+  size_t o_vec = take((P->fp64 ? 32 : 16) * npairs);
+  size_t o_img = P->keep_images ? take(4 * npairs) : 0;
+  size_t o_G = take(tsz * nsf_pad * N);
+  size_t o_dG = take(tsz * nsf_pad * N);
+  size_t o_E = take(8 * (size_t)N);
+  size_t o_F = take(4 * tsz * (size_t)N);
+  size_t o_Es = take(8 * (size_t)P->nstruc);
+  size_t o_V = take(72 * (size_t)P->nstruc);
+  size_t o_st = take(16);
+  if (cudaMalloc(&P->mem, off) != cudaSuccess) return AENET_ERR_CUDA;
+  P->mem_bytes = off;
+  char* b = (char*)P->mem;
+  P->geom_d = (StructGeom*)(b + o_geom);
+  P->atom_struct = (int*)(b + o_as);
+  P->types0 = (int*)(b + o_t0);
+  P->s_wrap = (double*)(b + o_s);
+  P->r_wrap = (double*)(b + o_r);
+  P->r_f32 = (float4*)(b + o_rf);
+  P->cell_of = (int*)(b + o_co);
+  P->cell_count = (int*)(b + o_cc);
+  P->cell_atoms = (int*)(b + o_ca);
+  P->nb_cnt = (int*)(b + o_nc);
+  P->nb_jt = (int*)(b + o_jt);
+  P->nb_vec = (void*)(b + o_vec);
+  P->nb_img = P->keep_images ? (int*)(b + o_img) : nullptr;
+  P->G = (void*)(b + o_G);
+  P->dEdG = (void*)(b + o_dG);
+  P->E_atom = (double*)(b + o_E);
+  P->Facc = (void*)(b + o_F);
+  P->E_struct = (double*)(b + o_Es);
+  P->virial = (double*)(b + o_V);
+  P->status = (unsigned*)(b + o_st);
+  std::vector<int> as(N);
+  for (int s = 0, a = 0; s < P->nstruc; ++s)
+    for (int q = 0; q < P->natoms_h[s]; ++q) as[a++] = s;
+  cudaMemcpy(P->geom_d, P->geom_h.data(), sizeof(StructGeom) * P->nstruc, cudaMemcpyHostToDevice);
+  if (N) cudaMemcpy(P->atom_struct, as.data(), 4 * (size_t)N, cudaMemcpyHostToDevice);
+  cudaMemset(P->status, 0, 16);
+  if (cudaDeviceSynchronize() != cudaSuccess) return AENET_ERR_CUDA;
+  return 0;
+}
+
+aenet_gpu_plan* plan_new(int nstruc, const int* natoms, const double* lattices, const int* pbc,
+                         const double* coords0, int precision, const PotDevice* pd, double rc,
+                         int cap, bool keep_images, int* stat) {
+  auto P = std::make_unique<aenet_gpu_plan>();
+  P->nstruc = nstruc;
+  P->fp64 = precision == AENET_GPU_FP64 ? 1 : 0;
+  P->natoms_h.assign(natoms, natoms + nstruc);
+  P->pbc_h.assign(nstruc, 1);
+  if (pbc)
+    for (int s = 0; s < nstruc; ++s) P->pbc_h[s] = pbc[s] ? 1 : 0;
+  for (int s = 0; s < nstruc; ++s)
+    if (natoms[s] < 0 || (P->pbc_h[s] && !lattices)) {
+      *stat = AENET_ERR_INPUT;
+      return nullptr;
+    }
+  P->geom_h.resize(nstruc);
+  P->pd = pd;
+  P->rc = rc;
+  P->cell_div = g.cell_div;
+  P->cap = cap;
+  P->keep_images = keep_images;
+  int st = plan_alloc(P.get(), coords0, lattices);
+  if (st) {
+    *stat = st;
+    return nullptr;
+  }
+  *stat = 0;
+  return P.release();
+}
+
+DescBuffers desc_buffers(aenet_gpu_plan* P, const double* grad_scale, bool virial) {
+  DescBuffers d{};
+  d.natoms = P->natoms;
+  d.types = P->types0;
+  d.nb_cnt = P->nb_cnt;
+  d.nb_jt = P->nb_jt;
+  d.nb_vec = P->nb_vec;
+  d.cap = P->cap;
+  d.G = P->G;
+  d.dEdG = P->dEdG;
+  d.E_atom = P->E_atom;
+  d.F = P->Facc;
+  d.virial = virial ? P->virial : nullptr;
+  d.atom_struct = P->atom_struct;
+  d.grad_scale = grad_scale;
+  d.status = P->status;
+  return d;
+}
+
+NbBuffers nb_buffers(aenet_gpu_plan* P) {
+  NbBuffers nb{};
+  nb.geom = P->geom_d;
+  nb.atom_struct = P->atom_struct;
+  nb.s_wrap = P->s_wrap;
+  nb.r_wrap = P->r_wrap;
+  nb.r_f32 = P->r_f32;
+  nb.cell_of = P->cell_of;
+  nb.cell_count = P->cell_count;
+  nb.cell_atoms = P->cell_atoms;
+  nb.ncells_total = P->ncells;
+  nb.nstruc = P->nstruc;
+  nb.cap = P->cap;
+  nb.nb_cnt = P->nb_cnt;
+  nb.nb_jt = P->nb_jt;
+  nb.nb_vec = P->nb_vec;
+  nb.nb_img = P->nb_img;
+  nb.status = P->status;
+  return nb;
+}
+
+int ck(int e) { return e ? AENET_ERR_CUDA : 0; }
+
+// neighbours + descriptors + networks + energies
+int plan_forward(aenet_gpu_plan* P, const double* d_coords, const int* d_types, double* d_E,
+                 double* d_E_atoms, cudaStream_t s) {
+  const PotDevice& pd = *P->pd;
+  if (ck(ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s))) return AENET_ERR_CUDA;
+  NbBuffers nb = nb_buffers(P);
+  if (ck(ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s))) return AENET_ERR_CUDA;
+  DescBuffers d = desc_buffers(P, nullptr, false);
+  int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
+                                             : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
+  if (ck(e)) return AENET_ERR_CUDA;
+  if (ck(ae_launch_mlp(pd, d, P->fp64, s))) return AENET_ERR_CUDA;
+  if (ck(ae_launch_energy_reduce(P->nstruc, P->geom_d, P->E_atom, P->E_struct, s))) return AENET_ERR_CUDA;
+  if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
+    return AENET_ERR_CUDA;
+  if (d_E_atoms &&
+      cudaMemcpyAsync(d_E_atoms, P->E_atom, 8 * (size_t)P->natoms, cudaMemcpyDeviceToDevice, s))
+    return AENET_ERR_CUDA;
+  return 0;
+}
+
+int plan_adjoint(aenet_gpu_plan* P, const double* grad_scale, double* d_out, double out_sign,
+                 double* d_virial, cudaStream_t s) {
+  const PotDevice& pd = *P->pd;
+  const size_t tsz = P->fp64 ? 8 : 4;
+  if (cudaMemsetAsync(P->Facc, 0, 4 * tsz * (size_t)P->natoms, s)) return AENET_ERR_CUDA;
+  if (d_virial && cudaMemsetAsync(P->virial, 0, 72 * (size_t)P->nstruc, s)) return AENET_ERR_CUDA;
+  DescBuffers d = desc_buffers(P, grad_scale, d_virial != nullptr);
+  int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, P->fp64, s)
+                                             : ae_launch_chebyshev_adjoint(pd, d, P->fp64, s);
+  if (ck(e)) return AENET_ERR_CUDA;
+  if (d_out && ck(ae_launch_forces_out(P->natoms, P->Facc, P->fp64, d_out, out_sign, s)))
+    return AENET_ERR_CUDA;
+  if (d_virial &&
+      cudaMemcpyAsync(d_virial, P->virial, 72 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
+    return AENET_ERR_CUDA;
+  return 0;
+}
+
+}  // namespace
+
+// =====================================================================
+//                     libaenet API (include/aenet.h)
+// =====================================================================
+
+EXPORT void aenet_init(int ntypes, char* atom_types[], int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g.init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  if (ntypes < 1 || ntypes > AE_MAXT || !atom_types) {
+    *stat = AENET_ERR_MALLOC;
+    return;
+  }
+  g.pots.clear();
+  g.types.clear();
+  g.blob.reset();
+  g.dev_ready = false;
+  g.loaded = false;
+  g.ntypes = ntypes;
+  for (int i = 0; i < ntypes; ++i) {
+    char buf[3] = {0, 0, 0};
+    if (atom_types[i]) strncpy(buf, atom_types[i], 2);
+    g.types.push_back(trim(buf));
+  }
+  g.pots.assign(ntypes, HostPot());
+  g.init = true;
+  *stat = AENET_OK;
+}
+
+EXPORT void aenet_final(int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  *stat = AENET_OK;
+  if (g.init) {
+    g_cache.reset();
+    g.blob.reset();
+    g.pots.clear();
+    g.types.clear();
+    g.init = false;
+    g.loaded = false;
+    g.dev_ready = false;
+    g.ntypes = 0;
+  }
+}
+
+EXPORT void aenet_print_info(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init) {
+    printf(" Nothing to print. AenetLib is not initialized.\n");
+    return;
+  }
+  for (int t = 0; t < g.ntypes; ++t) {
+    const HostPot& p = g.pots[t];
+    if (!p.init) continue;
+    printf(" Atomic species : %s\n File name      : %s\n\n", p.stp.atomtype.c_str(), p.path.c_str());
+    printf(" Network        :");
+    for (int l = 0; l < p.net.nlayers; ++l) printf(" %d", p.net.nnodes[l]);
+    printf("\n Descriptor     : %s, %d functions, Rc = %.3f\n", p.stp.sftype.c_str(), p.stp.nsf,
+           p.stp.Rc_max);
+    printf(" E_scale, E_shift, E_atom : %.10g %.10g %.10g\n\n", p.E_scale, p.E_shift, p.E_atom);
+  }
+}
+
+EXPORT void aenet_load_potential(int type_id, char* filename, int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!filename) {
+    *stat = AENET_ERR_IO;
+    return;
+  }
+  if (strlen(filename) > 1024) {   // aenet.f90:303-307
+    *stat = AENET_ERR_MALLOC;
+    return;
+  }
+  if (!g.init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  if (type_id <= 0 || type_id > g.ntypes) {
+    *stat = AENET_ERR_TYPE;
+    return;
+  }
+  std::string path = trim(filename);
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) {
+    *stat = AENET_ERR_IO;
+    return;
+  }
+  fclose(f);
+  HostPot pot;
+  int st = load_nn(path.c_str(), g.types, pot);
+  if (st) {
+    *stat = AENET_ERR_IO;
+    return;
+  }
+  g.pots[type_id - 1] = std::move(pot);
+  g.dev_ready = false;
+  bool all = true;
+  for (auto& p : g.pots) all = all && p.init;
+  if (all) {
+    // pot_get_range (potential.f90:244-266), lcl_nmax_nbdist, stp_nsf_max
+    double rmin = g.pots[0].stp.Rc_min, rmax = g.pots[0].stp.Rc_max;
+    int nsf = 0;
+    for (auto& p : g.pots) {
+      rmin = std::min(rmin, p.stp.Rc_min);
+      rmax = std::max(rmax, p.stp.Rc_max);
+      nsf = std::max(nsf, p.stp.nsf);
+    }
+    aenet_Rc_min = rmin;
+    aenet_Rc_max = rmax;
+    aenet_nnb_max = nmax_nbdist(rmin, rmax);
+    aenet_nsf_max = nsf;
+    g.loaded = true;
+  }
+  *stat = AENET_OK;
+}
+
+EXPORT bool aenet_all_loaded(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init) return true;   // empty loop over zero potentials
+  for (auto& p : g.pots)
+    if (!p.init) return false;
+  return true;
+}
+
+EXPORT double aenet_free_atom_energy(int type_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init || type_id < 1 || type_id > g.ntypes) return 0.0;
+  return g.pots[type_id - 1].E_atom;
+}
+
+namespace {
+
+// One atom with caller-supplied neighbours, evaluated on the GPU as a
+// one-row neighbour table (aenet.f90:359-486).  F_local[(n_j+1)*3]
+// receives the forces on the central atom (row 0) and on each neighbour.
+int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, const int* type_j,
+                double* E_i, double* F_local) {
+  if (!(g.init && g.loaded)) return AENET_ERR_INIT;
+  if (type_i < 1 || type_i > g.ntypes || n_j < 0) return AENET_ERR_TYPE;
+  for (int j = 0; j < n_j; ++j)
+    if (type_j[j] < 1 || type_j[j] > g.ntypes) return AENET_ERR_TYPE;
+  int st = ensure_device();
+  if (st) return st;
+  const PotDevice& pd = g.pd;
+  const int cap = std::max(32, (n_j + 31) & ~31);
+  const bool fp64 = true;
+  // host neighbour row: R_ij = coo_j - coo_i (sfbasis.f90:488)
+  std::vector<double> vec(4 * (size_t)cap, 0.0);
+  std::vector<int> jt(cap, 0);
+  for (int j = 0; j < n_j; ++j) {
+    double R[3];
+    for (int c = 0; c < 3; ++c) R[c] = coo_j[3 * j + c] - coo_i[c];
+    vec[4 * j] = R[0];
+    vec[4 * j + 1] = R[1];
+    vec[4 * j + 2] = R[2];
+    vec[4 * j + 3] = std::sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+    jt[j] = (j + 1) | ((type_j[j] - 1) << AE_TYPE_SHIFT);
+  }
+  const size_t nsf_pad = pd.nsf_pad;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = (off + bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  size_t o_vec = take(32 * (size_t)cap), o_jt = take(4 * (size_t)cap), o_cnt = take(4),
+         o_t = take(4), o_as = take(4), o_G = take(8 * nsf_pad), o_dG = take(8 * nsf_pad),
+         o_E = take(8), o_F = take(32 * (size_t)(n_j + 1)), o_st = take(16);
+  void* mem = nullptr;
+  if (cudaMalloc(&mem, off) != cudaSuccess) return AENET_ERR_MALLOC;
+  char* b = (char*)mem;
+  int zero = 0, t0 = type_i - 1, one = n_j;
+  cudaMemcpy(b + o_vec, vec.data(), 32 * (size_t)cap, cudaMemcpyHostToDevice);
+  cudaMemcpy(b + o_jt, jt.data(), 4 * (size_t)cap, cudaMemcpyHostToDevice);
+  cudaMemcpy(b + o_cnt, &one, 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(b + o_t, &t0, 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(b + o_as, &zero, 4, cudaMemcpyHostToDevice);
+  cudaMemset(b + o_F, 0, 32 * (size_t)(n_j + 1));
+  cudaMemset(b + o_st, 0, 16);
+  DescBuffers d{};
+  d.natoms = 1;
+  d.types = (const int*)(b + o_t);
+  d.nb_cnt = (const int*)(b + o_cnt);
+  d.nb_jt = (const int*)(b + o_jt);
+  d.nb_vec = b + o_vec;
+  d.cap = cap;
+  d.G = b + o_G;
+  d.dEdG = b + o_dG;
+  d.E_atom = (double*)(b + o_E);
+  d.F = b + o_F;
+  d.virial = nullptr;
+  d.atom_struct = (const int*)(b + o_as);
+  d.grad_scale = nullptr;
+  d.status = (unsigned*)(b + o_st);
+  cudaStream_t s = 0;
+  int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, fp64, s)
+                                             : ae_launch_chebyshev_forward(pd, d, fp64, s);
+  if (!e) e = ae_launch_mlp(pd, d, fp64, s);
+  if (!e && F_local)
+    e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, fp64, s)
+                                           : ae_launch_chebyshev_adjoint(pd, d, fp64, s);
+  if (!e) e = (int)cudaMemcpy(E_i, b + o_E, 8, cudaMemcpyDeviceToHost);
+  if (!e && F_local) {
+    std::vector<double> f4(4 * (size_t)(n_j + 1));
+    e = (int)cudaMemcpy(f4.data(), b + o_F, f4.size() * 8, cudaMemcpyDeviceToHost);
+    for (int q = 0; q <= n_j; ++q)
+      for (int c = 0; c < 3; ++c) F_local[3 * q + c] = f4[4 * q + c];
+  }
+  cudaFree(mem);
+  return e ? AENET_ERR_CUDA : 0;
+}
+
+}  // namespace
+
+EXPORT void aenet_atomic_energy(double coo_i[3], int type_i, int n_j, double coo_j[],
+                                int type_j[], double* E_i, int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  *stat = atomic_eval(coo_i, type_i, n_j, coo_j, type_j, E_i, nullptr);
+}
+
+EXPORT void aenet_atomic_energy_and_forces(double coo_i[3], int type_i, int index_i, int n_j,
+                                           double coo_j[], int type_j[], int index_j[],
+                                           int natoms, double* E_i, double F[], int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (index_i < 1 || index_i > natoms) {
+    *stat = AENET_ERR_INPUT;
+    return;
+  }
+  for (int j = 0; j < n_j; ++j)
+    if (index_j[j] < 1 || index_j[j] > natoms) {
+      *stat = AENET_ERR_INPUT;
+      return;
+    }
+  std::vector<double> Fl(3 * (size_t)(n_j + 1));
+  int st = atomic_eval(coo_i, type_i, n_j, coo_j, type_j, E_i, Fl.data());
+  if (st) {
+    *stat = st;
+    return;
+  }
+  // accumulate into the caller's F (aenet.f90:471-477)
+  for (int c = 0; c < 3; ++c) F[3 * (index_i - 1) + c] += Fl[c];
+  for (int j = 0; j < n_j; ++j)
+    for (int c = 0; c < 3; ++c) F[3 * (index_j[j] - 1) + c] += Fl[3 * (j + 1) + c];
+  *stat = AENET_OK;
+}
+
+EXPORT void aenet_convert_atom_types(int ntypes_in, char* atom_types[], int natoms_in,
+                                     int type_id_in[], int type_id_out[], int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  // geo_type_conv: map by name from the input type list to the library's
+  for (int i = 0; i < natoms_in; ++i) {
+    int t = type_id_in[i];
+    if (t < 1 || t > ntypes_in || !atom_types[t - 1]) {
+      *stat = AENET_ERR_TYPE;
+      return;
+    }
+    char buf[3] = {0, 0, 0};
+    strncpy(buf, atom_types[t - 1], 2);
+    std::string name = trim(buf);
+    int out = 0;
+    for (int q = 0; q < g.ntypes; ++q)
+      if (g.types[q] == name) {
+        out = q + 1;
+        break;
+      }
+    if (!out) {
+      *stat = AENET_ERR_TYPE;
+      return;
+    }
+    type_id_out[i] = out;
+  }
+  *stat = AENET_OK;
+}
+
+// ---- stand-alone Chebyshev basis (aenet.f90:652-799) ----------------
+
+EXPORT void aenet_sfb_init(int ntypes, char* atom_types[], int radial_order, int angular_order,
+                           double radial_Rc, double angular_Rc, int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  (void)atom_types;
+  if (g.sfb_init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  if (ntypes < 1 || ntypes > AE_MAXT || radial_order < 0 || angular_order < 0 ||
+      radial_order + 1 > AE_MAXCHEB || angular_order + 1 > AE_MAXCHEB) {
+    *stat = AENET_ERR_INPUT;
+    return;
+  }
+  if (!cuda_ok()) {
+    *stat = AENET_ERR_CUDA;
+    return;
+  }
+  PotDevice pd{};
+  pd.ntypes = 1;
+  ChebTable& ct = pd.sp[0].cheb;
+  pd.sp[0].sftype = AE_SF_CHEBYSHEV;
+  ct.r_Rc = radial_Rc;
+  ct.a_Rc = angular_Rc;
+  ct.r_N = radial_order + 1;
+  ct.a_N = angular_order + 1;
+  ct.multi = ntypes > 1;
+  ct.nsf = (ct.r_N + ct.a_N) * (ct.multi ? 2 : 1);
+  ct.r_i1 = 0;
+  ct.a_i1 = ct.r_N;
+  ct.r_i2 = ct.r_N + ct.a_N;
+  ct.a_i2 = 2 * ct.r_N + ct.a_N;
+  ct.angular_legacy = g.angular_legacy;
+  for (int t = 0; t < ntypes; ++t) ct.spin[t] = typespin(ntypes, t + 1);
+  pd.sp[0].nsf = ct.nsf;
+  pd.nsf_max = ct.nsf;
+  pd.nsf_pad = (ct.nsf + 3) & ~3;
+  std::vector<double> shift(pd.nsf_pad, 0.0), scale(pd.nsf_pad, 1.0);
+  std::vector<float> shift2(2 * (size_t)pd.nsf_pad, 0.f), scale32(pd.nsf_pad, 1.f);
+  auto blob = std::make_unique<DevBlob>();
+  if (cudaMalloc(&blob->p, 28 * (size_t)pd.nsf_pad) != cudaSuccess) {
+    *stat = AENET_ERR_CUDA;
+    return;
+  }
+  cudaMemcpy(blob->p, shift.data(), 8 * (size_t)pd.nsf_pad, cudaMemcpyHostToDevice);
+  cudaMemcpy((char*)blob->p + 8 * (size_t)pd.nsf_pad, scale.data(), 8 * (size_t)pd.nsf_pad,
+             cudaMemcpyHostToDevice);
+  cudaMemcpy((char*)blob->p + 16 * (size_t)pd.nsf_pad, shift2.data(), 8 * (size_t)pd.nsf_pad,
+             cudaMemcpyHostToDevice);
+  cudaMemcpy((char*)blob->p + 24 * (size_t)pd.nsf_pad, scale32.data(), 4 * (size_t)pd.nsf_pad,
+             cudaMemcpyHostToDevice);
+  pd.shift = (const double*)blob->p;
+  pd.scale = (const double*)((char*)blob->p + 8 * (size_t)pd.nsf_pad);
+  pd.shift2 = (const float2*)((char*)blob->p + 16 * (size_t)pd.nsf_pad);
+  pd.scale32 = (const float*)((char*)blob->p + 24 * (size_t)pd.nsf_pad);
+  g.sfb_pd = pd;
+  g.sfb_blob = std::move(blob);
+  g.sfb_ntypes = ntypes;
+  g.sfb_rorder = radial_order;
+  g.sfb_aorder = angular_order;
+  g.sfb_rRc = radial_Rc;
+  g.sfb_aRc = angular_Rc;
+  g.sfb_init = true;
+  *stat = AENET_OK;
+}
+
+EXPORT void aenet_sfb_final(int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.sfb_init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  g.sfb_blob.reset();
+  g.sfb_init = false;
+  *stat = AENET_OK;
+}
+
+EXPORT int aenet_sfb_nvalues(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g.sfb_init ? g.sfb_pd.sp[0].cheb.nsf : 0;
+}
+
+EXPORT void aenet_sfb_eval(int itype0, double coo0[3], int nat, int itype1[], double coo1[], int nv,
+                           double values[], int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  (void)itype0;
+  if (!g.sfb_init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  const PotDevice& pd = g.sfb_pd;
+  if (nv != pd.sp[0].cheb.nsf || nat < 0) {
+    *stat = AENET_ERR_INPUT;
+    return;
+  }
+  for (int j = 0; j < nat; ++j)
+    if (itype1[j] < 1 || itype1[j] > g.sfb_ntypes) {
+      *stat = AENET_ERR_TYPE;
+      return;
+    }
+  const int cap = std::max(32, (nat + 31) & ~31);
+  std::vector<double> vec(4 * (size_t)cap, 0.0);
+  std::vector<int> jt(cap, 0);
+  for (int j = 0; j < nat; ++j) {
+    double R[3];
+    for (int c = 0; c < 3; ++c) R[c] = coo1[3 * j + c] - coo0[c];
+    for (int c = 0; c < 3; ++c) vec[4 * j + c] = R[c];
+    vec[4 * j + 3] = std::sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+    jt[j] = (j + 1) | ((itype1[j] - 1) << AE_TYPE_SHIFT);
+  }
+  size_t nsf_pad = pd.nsf_pad;
+  void* mem = nullptr;
+  size_t bytes = 32 * (size_t)cap + 4 * (size_t)cap + 64 + 16 * nsf_pad + 1024;
+  if (cudaMalloc(&mem, bytes) != cudaSuccess) {
+    *stat = AENET_ERR_CUDA;
+    return;
+  }
+  char* b = (char*)mem;
+  char* p_vec = b;
+  char* p_jt = p_vec + 32 * (size_t)cap;
+  char* p_small = p_jt + 4 * (size_t)cap;  // cnt, type, struct
+  char* p_G = p_small + 256;
+  int small[3] = {nat, 0, 0};
+  cudaMemcpy(p_vec, vec.data(), 32 * (size_t)cap, cudaMemcpyHostToDevice);
+  cudaMemcpy(p_jt, jt.data(), 4 * (size_t)cap, cudaMemcpyHostToDevice);
+  cudaMemcpy(p_small, small, 12, cudaMemcpyHostToDevice);
+  DescBuffers d{};
+  d.natoms = 1;
+  d.nb_cnt = (const int*)p_small;
+  d.types = (const int*)(p_small + 4);
+  d.atom_struct = (const int*)(p_small + 8);
+  d.nb_jt = (const int*)p_jt;
+  d.nb_vec = p_vec;
+  d.cap = cap;
+  d.G = p_G;
+  int e = ae_launch_chebyshev_forward(pd, d, 1, 0);
+  std::vector<double> out(nsf_pad);
+  if (!e) e = (int)cudaMemcpy(out.data(), p_G, 8 * nsf_pad, cudaMemcpyDeviceToHost);
+  cudaFree(mem);
+  if (e) {
+    *stat = AENET_ERR_CUDA;
+    return;
+  }
+  for (int k = 0; k < nv; ++k) values[k] = out[k];
+  *stat = AENET_OK;
+}
+
+// sfb_reconstruct_radial (sfbasis.f90:581-637): a host-side utility of
+// the descriptor basis, not part of the energy/force path.
+EXPORT void aenet_sfb_reconstruct_radial(int nv, double values[], int nx, double x[], double y[],
+                                         int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.sfb_init) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  const double PI = 3.14159265358979;
+  const int rN = g.sfb_rorder + 1;
+  if (nv < rN || nx < 2) {
+    *stat = AENET_ERR_INPUT;
+    return;
+  }
+  const double Rc = g.sfb_rRc;
+  double dx = Rc / (double)(nx - 1);
+  for (int ix = 0; ix < nx; ++ix) x[ix] = (double)ix * dx;
+  std::vector<double> f(rN);
+  for (int ix = 0; ix < nx - 1; ++ix) {
+    double xx = (2.0 * x[ix] - 0.0 - Rc) / (Rc - 0.0);
+    f[0] = 1.0;
+    if (rN > 1) f[1] = xx;
+    for (int i = 2; i < rN; ++i) f[i] = 2.0 * xx * f[i - 1] - f[i - 2];
+    double r = x[ix] / Rc;
+    double w = 0.5 / std::sqrt(r - r * r);
+    for (int i = 0; i < rN; ++i) f[i] = f[i] * w * (1.0 / PI);
+    f[0] = 0.5 * f[0];
+    y[ix] = 0.0;
+    for (int ic = rN - 1; ic >= 0; --ic) y[ix] = y[ix] + values[ic] * f[ic];
+  }
+  y[nx - 1] = 0.0;
+  *stat = AENET_OK;
+}
+
+// ---- neighbour list API (aenet.f90:571-639) --------------------------
+
+EXPORT void aenet_nbl_init(double latt_vec[9], int natoms, int atom_types[], double coords[],
+                           bool cartesian, bool pbc) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g.nbl_init = false;
+  if (natoms < 1 || !g.loaded || !cuda_ok()) return;
+  int nat = natoms;
+  int pbcv = pbc ? 1 : 0;
+  // latt_vec is Fortran latticeVec(3,3): columns are vectors == rows here
+  aenet_gpu_plan* P = nullptr;
+  {
+    auto Pn = std::make_unique<aenet_gpu_plan>();
+    Pn->nstruc = 1;
+    Pn->fp64 = 1;
+    Pn->natoms_h = {nat};
+    Pn->pbc_h = {pbcv};
+    Pn->geom_h.resize(1);
+    Pn->pd = nullptr;
+    Pn->rc = aenet_Rc_max;
+    Pn->cell_div = g.cell_div;
+    Pn->keep_images = true;
+    // isolated structures are binned on the Cartesian input
+    int st = make_geom(Pn->geom_h[0], latt_vec, pbcv, coords, nat, aenet_Rc_max, g.cell_div,
+                       cartesian ? 1 : 2);
+    if (st) return;
+    // plan_alloc recomputes the geometry with frac_mode 0; redo with the
+    // nbl convention afterwards
+    StructGeom keep = Pn->geom_h[0];
+    if (plan_alloc(Pn.get(), coords, latt_vec)) return;
+    keep.cell_cap = Pn->geom_h[0].cell_cap;
+    keep.cell_off = 0;
+    keep.slot_off = 0;
+    keep.atom_off = 0;
+    Pn->geom_h[0] = keep;
+    cudaMemcpy(Pn->geom_d, &keep, sizeof(StructGeom), cudaMemcpyHostToDevice);
+    P = Pn.release();
+  }
+  std::unique_ptr<aenet_gpu_plan> hold(P);
+  double* d_c = nullptr;
+  int* d_t = nullptr;
+  cudaMalloc(&d_c, 24 * (size_t)nat);
+  cudaMalloc(&d_t, 4 * (size_t)nat);
+  cudaMemcpy(d_c, coords, 24 * (size_t)nat, cudaMemcpyHostToDevice);
+  cudaMemcpy(d_t, atom_types, 4 * (size_t)nat, cudaMemcpyHostToDevice);
+  int ntmax = g.ntypes;
+  ae_launch_types(nat, d_t, P->types0, ntmax, P->status, 0);
+  NbBuffers nb = nb_buffers(P);
+  ae_launch_neighbors(nat, d_c, P->types0, nb, 1, 0);
+  g.nbl_cnt.resize(nat);
+  g.nbl_jt.resize((size_t)nat * P->cap);
+  g.nbl_img.resize((size_t)nat * P->cap);
+  g.nbl_vec.resize((size_t)nat * P->cap * 4);
+  g.nbl_s.resize(3 * (size_t)nat);
+  g.nbl_cart.resize(3 * (size_t)nat);
+  cudaMemcpy(g.nbl_cnt.data(), P->nb_cnt, 4 * (size_t)nat, cudaMemcpyDeviceToHost);
+  cudaMemcpy(g.nbl_jt.data(), P->nb_jt, 4 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost);
+  cudaMemcpy(g.nbl_img.data(), P->nb_img, 4 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost);
+  cudaMemcpy(g.nbl_vec.data(), P->nb_vec, 32 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost);
+  cudaMemcpy(g.nbl_s.data(), P->s_wrap, 24 * (size_t)nat, cudaMemcpyDeviceToHost);
+  cudaMemcpy(g.nbl_cart.data(), P->r_wrap, 24 * (size_t)nat, cudaMemcpyDeviceToHost);
+  unsigned status = 0;
+  cudaMemcpy(&status, P->status, 4, cudaMemcpyDeviceToHost);
+  cudaFree(d_c);
+  cudaFree(d_t);
+  if (cudaDeviceSynchronize() != cudaSuccess || status) return;
+  g.nbl_natoms = nat;
+  g.nbl_types.assign(atom_types, atom_types + nat);
+  memcpy(g.nbl_L, latt_vec, sizeof(g.nbl_L));
+  g.nbl_pbc = pbcv;
+  // coords = matmul(latt_vec, coo_latt) (aenet.f90:605)
+  for (size_t q = 0; q < 3 * (size_t)nat; ++q) coords[q] = g.nbl_cart[q];
+  g.nbl_cap = P->cap;
+  g.nbl_init = true;
+}
+
+EXPORT void aenet_nbl_final(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  g.nbl_init = false;
+  g.nbl_cnt.clear();
+  g.nbl_jt.clear();
+  g.nbl_img.clear();
+  g.nbl_vec.clear();
+}
+
+EXPORT void aenet_nbl_neighbors(int iatom, int* nnb, double nbcoo[], double nbdist[], int nblist[],
+                                int nbtype[]) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.nbl_init || iatom < 1 || iatom > g.nbl_natoms) {
+    *nnb = 0;
+    return;
+  }
+  const int cap = g.nbl_cap;
+  const int i = iatom - 1;
+  const int n = g.nbl_cnt[i];
+  const int lim = std::min(n, *nnb);
+  for (int k = 0; k < lim; ++k) {
+    size_t q = (size_t)i * cap + k;
+    int j = g.nbl_jt[q] & AE_INDEX_MASK;
+    int img = g.nbl_img[q];
+    int T[3];
+    for (int c = 0; c < 3; ++c) {
+      int v = (img >> (10 * c)) & 1023;
+      T[c] = v >= 512 ? v - 1024 : v;
+    }
+    // nbcoo = latticeVec (s_j + T) (lclist.f90:606-611, 646-650)
+    for (int c = 0; c < 3; ++c) {
+      if (g.nbl_pbc) {
+        double u0 = g.nbl_s[3 * j] + (double)T[0], u1 = g.nbl_s[3 * j + 1] + (double)T[1],
+               u2 = g.nbl_s[3 * j + 2] + (double)T[2];
+        double t = g.nbl_L[c] * u0;
+        t = t + g.nbl_L[3 + c] * u1;
+        t = t + g.nbl_L[6 + c] * u2;
+        nbcoo[3 * k + c] = t;
+      } else {
+        nbcoo[3 * k + c] = g.nbl_cart[3 * j + c];
+      }
+    }
+    nbdist[k] = g.nbl_vec[4 * q + 3];
+    nblist[k] = j + 1;
+    nbtype[k] = g.nbl_types[j];
+  }
+  *nnb = lim;
+}
+
+// =====================================================================
+//                 batched extensions (include/aenet_gb300.h)
+// =====================================================================
+
+EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!key || !value) return AENET_ERR_INPUT;
+  std::string k = key, v = value;
+  if (k == "angular_domain") {
+    if (v == "legacy") g.angular_legacy = 1;
+    else if (v == "current") g.angular_legacy = 0;
+    else return AENET_ERR_INPUT;
+    g.dev_ready = false;
+    return AENET_OK;
+  }
+  if (k == "cell_div") {
+    int d = atoi(v.c_str());
+    if (d < 1 || d > 3) return AENET_ERR_INPUT;
+    g.cell_div = d;
+    return AENET_OK;
+  }
+  return AENET_ERR_INPUT;
+}
+
+EXPORT aenet_gpu_plan* aenet_gpu_plan_create(int nstruc, const int* natoms, const double* lattices,
+                                             const int* pbc, const double* coords0, int precision,
+                                             int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (nstruc < 1 || !natoms) {
+    *stat = AENET_ERR_INPUT;
+    return nullptr;
+  }
+  int st = ensure_device();
+  if (st) {
+    *stat = st;
+    return nullptr;
+  }
+  return plan_new(nstruc, natoms, lattices, pbc, coords0, precision, &g.pd, aenet_Rc_max, 0, false,
+                  stat);
+}
+
+EXPORT void aenet_gpu_plan_destroy(aenet_gpu_plan* plan) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  delete plan;
+}
+
+EXPORT int aenet_gpu_plan_natoms(const aenet_gpu_plan* plan) { return plan ? plan->natoms : 0; }
+
+EXPORT int aenet_gpu_plan_set_lattices(aenet_gpu_plan* P, const double* lattices) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!P || !lattices) return AENET_ERR_INPUT;
+  for (int s = 0; s < P->nstruc; ++s) {
+    StructGeom G;
+    if (!P->pbc_h[s]) continue;
+    StructGeom& O = P->geom_h[s];
+    // the cell grid keeps its dimensions (the slot layout depends on them);
+    // the stencil half widths follow the new heights
+    int st = make_geom(G, lattices + 9 * (size_t)s, 1, nullptr, P->natoms_h[s], P->rc, P->cell_div,
+                       O.frac_mode, O.nc);
+    if (st) return st;
+    G.cell_cap = O.cell_cap;
+    G.cell_off = O.cell_off;
+    G.slot_off = O.slot_off;
+    G.atom_off = O.atom_off;
+    O = G;
+  }
+  if (cudaMemcpy(P->geom_d, P->geom_h.data(), sizeof(StructGeom) * P->nstruc, cudaMemcpyHostToDevice))
+    return AENET_ERR_CUDA;
+  return 0;
+}
+
+EXPORT int aenet_gpu_plan_run(aenet_gpu_plan* P, const double* d_coords, const int* d_types,
+                              double* d_E, double* d_E_atoms, double* d_F, double* d_virial,
+                              unsigned flags, void* stream) {
+  if (!P) return AENET_ERR_INPUT;
+  cudaStream_t s = (cudaStream_t)stream;
+  int st = plan_forward(P, d_coords, d_types, d_E, d_E_atoms, s);
+  if (st) return st;
+  if ((flags & (AENET_GPU_FORCES | AENET_GPU_VIRIAL)) || d_F || d_virial)
+    return plan_adjoint(P, nullptr, d_F, 1.0, (flags & AENET_GPU_VIRIAL) ? d_virial : nullptr, s);
+  return 0;
+}
+
+EXPORT int aenet_gpu_plan_forward(aenet_gpu_plan* P, const double* d_coords, const int* d_types,
+                                  double* d_E, double* d_E_atoms, void* stream) {
+  if (!P) return AENET_ERR_INPUT;
+  return plan_forward(P, d_coords, d_types, d_E, d_E_atoms, (cudaStream_t)stream);
+}
+
+EXPORT int aenet_gpu_plan_backward(aenet_gpu_plan* P, const double* d_weights, double* d_grad,
+                                   double* d_virial, void* stream) {
+  if (!P) return AENET_ERR_INPUT;
+  // the adjoint accumulates forces -dE/dR; the output is their negative
+  return plan_adjoint(P, d_weights, d_grad, -1.0, d_virial, (cudaStream_t)stream);
+}
+
+// Same pipeline as aenet_gpu_plan_run(..., AENET_GPU_FORCES) with CUDA
+// events recorded on `stream` between the stages; ms[0..6] receive the
+// durations of: type check, neighbour search, descriptor, networks,
+// energy reduction, adjoint (forces), force output.  Synchronises.
+EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, const int* d_types,
+                                  double* d_E, double* d_F, float* ms, void* stream) {
+  if (!P || !ms) return AENET_ERR_INPUT;
+  cudaStream_t s = (cudaStream_t)stream;
+  const PotDevice& pd = *P->pd;
+  cudaEvent_t ev[8];
+  for (int q = 0; q < 8; ++q) cudaEventCreate(&ev[q]);
+  int e = 0;
+  cudaEventRecord(ev[0], s);
+  e |= ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s);
+  cudaEventRecord(ev[1], s);
+  NbBuffers nb = nb_buffers(P);
+  e |= ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s);
+  cudaEventRecord(ev[2], s);
+  DescBuffers d = desc_buffers(P, nullptr, false);
+  e |= (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
+                                          : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
+  cudaEventRecord(ev[3], s);
+  e |= ae_launch_mlp(pd, d, P->fp64, s);
+  cudaEventRecord(ev[4], s);
+  e |= ae_launch_energy_reduce(P->nstruc, P->geom_d, P->E_atom, P->E_struct, s);
+  if (d_E) cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s);
+  cudaEventRecord(ev[5], s);
+  const size_t tsz = P->fp64 ? 8 : 4;
+  cudaMemsetAsync(P->Facc, 0, 4 * tsz * (size_t)P->natoms, s);
+  e |= (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, P->fp64, s)
+                                          : ae_launch_chebyshev_adjoint(pd, d, P->fp64, s);
+  cudaEventRecord(ev[6], s);
+  if (d_F) e |= ae_launch_forces_out(P->natoms, P->Facc, P->fp64, d_F, 1.0, s);
+  cudaEventRecord(ev[7], s);
+  if (cudaEventSynchronize(ev[7]) != cudaSuccess) e = 1;
+  for (int q = 0; q < 7; ++q) cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]);
+  for (int q = 0; q < 8; ++q) cudaEventDestroy(ev[q]);
+  return e ? AENET_ERR_CUDA : 0;
+}
+
+EXPORT unsigned aenet_gpu_plan_status(aenet_gpu_plan* P, void* stream) {
+  if (!P) return 0;
+  unsigned v = 0;
+  cudaMemcpyAsync(&v, P->status, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  cudaStreamSynchronize((cudaStream_t)stream);
+  return v;
+}
+
+EXPORT int aenet_gpu_plan_neighbors(aenet_gpu_plan* P, int* cap, const int** d_counts,
+                                    const int** d_jt, const void** d_vec) {
+  if (!P) return AENET_ERR_INPUT;
+  *cap = P->cap;
+  *d_counts = P->nb_cnt;
+  *d_jt = P->nb_jt;
+  *d_vec = P->nb_vec;
+  return 0;
+}
+
+EXPORT int aenet_gpu_plan_descriptors(aenet_gpu_plan* P, const void** d_G, int* nsf_pad) {
+  if (!P) return AENET_ERR_INPUT;
+  *d_G = P->G;
+  *nsf_pad = P->pd->nsf_pad;
+  return 0;
+}
+
+// ---- host-buffer entry points ----------------------------------------
+
+namespace {
+
+
+bool cache_matches(int nstruc, const int* natoms, const double* lattices, const int* pbc,
+                   int precision) {
+  HostPlanCache& c = g_cache;
+  if (!c.plan || c.precision != precision || (int)c.natoms.size() != nstruc || c.isolated) return false;
+  if (memcmp(c.natoms.data(), natoms, 4 * (size_t)nstruc)) return false;
+  for (int s = 0; s < nstruc; ++s)
+    if (c.pbc[s] != (pbc ? (pbc[s] ? 1 : 0) : 1)) return false;
+  if (lattices && memcmp(c.lattices.data(), lattices, 72 * (size_t)nstruc)) return false;
+  return true;
+}
+
+int batch_host(int nstruc, const int* natoms, const double* coords, const int* type_ids,
+               const double* lattices, const int* pbc, int precision, double* E,
+               double* E_atoms, double* F, double* virial, bool want_forces) {
+  int st = ensure_device();
+  if (st) return st;
+  int cap = 0;
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    HostPlanCache& c = g_cache;
+    if (!(attempt == 0 && cache_matches(nstruc, natoms, lattices, pbc, precision))) {
+      c.reset();
+      c.plan.reset(plan_new(nstruc, natoms, lattices, pbc, coords, precision, &g.pd, aenet_Rc_max,
+                            cap, false, &st));
+      if (!c.plan) return st;
+      c.natoms.assign(natoms, natoms + nstruc);
+      c.pbc.assign(nstruc, 1);
+      c.isolated = false;
+      for (int q = 0; q < nstruc; ++q) {
+        c.pbc[q] = pbc ? (pbc[q] ? 1 : 0) : 1;
+        if (!c.pbc[q]) c.isolated = true;   // binning box follows the coordinates
+      }
+      c.lattices.assign(lattices ? lattices : nullptr, lattices ? lattices + 9 * (size_t)nstruc : nullptr);
+      c.precision = precision;
+      if (!c.stream && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+        return AENET_ERR_CUDA;
+    }
+    aenet_gpu_plan* P = c.plan.get();
+    const int N = P->natoms;
+    double *d_c = nullptr, *d_E = nullptr, *d_Ea = nullptr, *d_F = nullptr, *d_V = nullptr;
+    int* d_t = nullptr;
+    size_t bytes = 24 * (size_t)N + 4 * (size_t)N + 8 * (size_t)nstruc + 8 * (size_t)N +
+                   24 * (size_t)N + 72 * (size_t)nstruc + 1024;
+    if (c.io_bytes < bytes) {
+      if (c.io) cudaFree(c.io);
+      c.io = nullptr;
+      if (cudaMalloc(&c.io, bytes) != cudaSuccess) return AENET_ERR_CUDA;
+      c.io_bytes = bytes;
+    }
+    char* mem = c.io;
+    d_c = (double*)mem;
+    d_F = d_c + 3 * (size_t)N;
+    d_Ea = d_F + 3 * (size_t)N;
+    d_E = d_Ea + N;
+    d_V = d_E + nstruc;
+    d_t = (int*)(d_V + 9 * (size_t)nstruc);
+    cudaStream_t s = c.stream;
+    cudaMemsetAsync(P->status, 0, 4, s);
+    cudaMemcpyAsync(d_c, coords, 24 * (size_t)N, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_t, type_ids, 4 * (size_t)N, cudaMemcpyHostToDevice, s);
+    unsigned flags = (want_forces ? AENET_GPU_FORCES : 0u) | (virial ? AENET_GPU_VIRIAL : 0u);
+    st = aenet_gpu_plan_run(P, d_c, d_t, d_E, E_atoms ? d_Ea : nullptr,
+                            (want_forces || virial) ? d_F : nullptr, virial ? d_V : nullptr, flags, s);
+    unsigned status = 0;
+    if (!st) {
+      cudaMemcpyAsync(&status, P->status, 4, cudaMemcpyDeviceToHost, s);
+      if (E) cudaMemcpyAsync(E, d_E, 8 * (size_t)nstruc, cudaMemcpyDeviceToHost, s);
+      if (E_atoms) cudaMemcpyAsync(E_atoms, d_Ea, 8 * (size_t)N, cudaMemcpyDeviceToHost, s);
+      if (F && want_forces) cudaMemcpyAsync(F, d_F, 24 * (size_t)N, cudaMemcpyDeviceToHost, s);
+      if (virial) cudaMemcpyAsync(virial, d_V, 72 * (size_t)nstruc, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) st = AENET_ERR_CUDA;
+    }
+    if (st) {
+      c.reset();
+      return st;
+    }
+    if (status & (AE_ST_BAD_COORD)) return AENET_ERR_INPUT;
+    if (status & AE_ST_BAD_TYPE) return AENET_ERR_TYPE;
+    if (status & (AE_ST_NB_OVERFLOW | AE_ST_CELL_OVERFLOW)) {
+      // retry with larger capacities
+      cap = P->cap * 2;
+      c.reset();
+      continue;
+    }
+    return 0;
+  }
+  return AENET_ERR_MALLOC;
+}
+
+}  // namespace
+
+EXPORT void aenet_gpu_structure_energy_forces(int natoms, const double* coords, const int* type_ids,
+                                              const double* lattice, int pbc, int precision,
+                                              double* E_total, double* E_coh, double* E_atoms,
+                                              double* F, double* virial, int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!(g.init && g.loaded)) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  if (natoms < 1 || !coords || !type_ids) {
+    *stat = AENET_ERR_INPUT;
+    return;
+  }
+  std::vector<double> Ea(natoms);
+  double E = 0;
+  int st = batch_host(1, &natoms, coords, type_ids, lattice, &pbc, precision, &E, Ea.data(), F,
+                      virial, F != nullptr);
+  if (st) {
+    *stat = st;
+    return;
+  }
+  if (E_total) *E_total = E;
+  if (E_atoms) memcpy(E_atoms, Ea.data(), 8 * (size_t)natoms);
+  if (E_coh) {
+    double c = E;
+    for (int i = 0; i < natoms; ++i) c -= g.pots[type_ids[i] - 1].E_atom;
+    *E_coh = c;
+  }
+  *stat = AENET_OK;
+}
+
+EXPORT void aenet_gpu_batch_energy_forces(int nstruc, const int* natoms, const double* coords,
+                                          const int* type_ids, const double* lattices, const int* pbc,
+                                          int precision, double* E, double* F, double* virial,
+                                          int* stat) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!(g.init && g.loaded)) {
+    *stat = AENET_ERR_INIT;
+    return;
+  }
+  if (nstruc < 1 || !natoms || !coords || !type_ids) {
+    *stat = AENET_ERR_INPUT;
+    return;
+  }
+  *stat = batch_host(nstruc, natoms, coords, type_ids, lattices, pbc, precision, E, nullptr, F,
+                     virial, F != nullptr);
+}

@@ -1,0 +1,186 @@
+// Shared definitions of the GB300 evaluator: device-side tables of the
+// loaded potentials, per-structure geometry records and kernel launchers.
+//
+// Layout conventions (all device memory):
+//   positions      double [N][3]   Cartesian, Angstrom
+//   types          int    [N]      0-based global species index
+//   neighbour table ELL with `cap` slots per atom:
+//       nb_jt  int    [N*cap]  neighbour atom index | (species << AE_TYPE_SHIFT)
+//       nb_vec T4     [N*cap]  (R_ij.x, R_ij.y, R_ij.z, |R_ij|), T = float|double
+//       nb_cnt int    [N]      number of valid slots
+//   descriptors    T      [N][nsf_pad]  normalised features
+//   dE/dG          T      [N][nsf_pad]  scaled by E_scale and the
+//                                       normalisation scale, so that the
+//                                       adjoint contracts raw descriptor
+//                                       derivatives with it
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define AE_MAXT 8            // species per potential set
+#define AE_MAXNSF 128        // descriptor length
+#define AE_MAXLAYERS 8       // network layers including input and output
+#define AE_MAXNODES 64       // nodes per hidden layer
+#define AE_MAXCHEB 32        // Chebyshev order + 1
+#define AE_TYPE_SHIFT 26
+#define AE_INDEX_MASK ((1 << AE_TYPE_SHIFT) - 1)
+#define AE_MAXG4 64          // Behler angular functions per triple type
+#define AE_MAXG2 64          // Behler radial functions per pair type
+
+// status bits written by kernels into a device word
+#define AE_ST_NB_OVERFLOW 1u
+#define AE_ST_BAD_COORD 2u
+#define AE_ST_BAD_TYPE 4u
+#define AE_ST_CELL_OVERFLOW 8u
+
+enum { AE_SF_CHEBYSHEV = 1, AE_SF_BEHLER = 2 };
+
+// ----------------------------------------------------------------------
+// Potential tables
+// ----------------------------------------------------------------------
+struct ChebTable {
+  double r_Rc, a_Rc;
+  int r_N, a_N;     // number of radial / angular functions (order + 1)
+  int multi;        // spin-weighted copy present
+  int nsf;
+  // feature offsets: [radial r_N][angular a_N][radial spin][angular spin]
+  int r_i1, a_i1, r_i2, a_i2;
+  float spin[AE_MAXT];          // typespin of each GLOBAL neighbour species
+  int angular_legacy;           // T_n((2cos - pi)/pi) instead of T_n(cos)
+};
+
+struct BehlerFn {     // one radial (G1..G3) or angular (G4, G5) function
+  double Rc, p1, p2, p3;  // G2: Rs, eta; G3: kappa; G4/G5: lambda, zeta, eta
+  int kind;               // 1..5
+  int out;                // feature index (reference order)
+};
+
+// Per central species: functions grouped by neighbour species (radial) and
+// neighbour species pair (angular), with the feature index each feeds.
+struct BehlerTable {
+  int nsf;
+  double rc_max;                      // largest Rc of any function
+  int rad_off[AE_MAXT + 1];           // into fn[] by neighbour species
+  int ang_off[AE_MAXT * AE_MAXT + 1]; // by (tj, tk) with tj <= tk
+  int nfn;
+  BehlerFn fn[1];                     // variable length (allocated larger)
+};
+
+struct NetTable {
+  int nlayers;
+  int nnodes[AE_MAXLAYERS];
+  int f_a[AE_MAXLAYERS];              // activation of layer l (l >= 1)
+  int w_off[AE_MAXLAYERS];            // offset of layer l -> l+1 weights
+  int pitch[AE_MAXLAYERS];            // row pitch (odd) of layer l weights
+  int wtotal;                         // padded weight count
+};
+
+struct SpeciesTable {
+  int sftype;
+  int nsf;
+  double E_scale, E_shift, E_atom;
+  ChebTable cheb;
+  NetTable net;
+  int behler_off;                     // byte offset of BehlerTable in blob
+};
+
+struct PotDevice {
+  int ntypes;
+  int nsf_max;
+  int nsf_pad;                        // row stride of descriptor arrays
+  double Rc_max;                      // neighbour cut-off (before +1e-3)
+  SpeciesTable sp[AE_MAXT];
+  // device pointers
+  const double* shift;                // [ntypes][nsf_pad] normalisation
+  const double* scale;                // [ntypes][nsf_pad]
+  // the same constants for FP32 kernels: shift as an unevaluated sum
+  // hi + lo of two floats (FP64 precision), scale rounded to float
+  const float2* shift2;               // [ntypes][nsf_pad]
+  const float* scale32;               // [ntypes][nsf_pad]
+  const double* w64;                  // weights, row-major W[o][k], pitch
+  const float* w32;
+  const unsigned char* behler_blob;   // BehlerTable per species
+};
+
+// ----------------------------------------------------------------------
+// Structures of a batch
+// ----------------------------------------------------------------------
+struct StructGeom {
+  double L[9];        // lattice vectors as rows: L[3*v + c]
+  double B[9];        // reciprocal rows incl. 2 pi: s_v = (B[v].r)/(2 pi)
+  double origin[3];   // isolated structures: corner of the binning box
+  double box[3];      // isolated structures: edge lengths of the box
+  float Lf[9];
+  double rc2;         // (Rc + 1e-3)^2, the neighbour predicate
+  float rc2_lo, rc2_hi;   // FP32 distances in [lo, hi] are decided in FP64
+  int pbc;
+  int frac_mode;      // 0: s = (B r)/(2 pi) (predict.x), 1: s = (B r)/(2 pi)
+                      // with B without 2 pi (aenet_nbl_init), 2: input is s
+  int nc[3];          // cell grid
+  int kr[3];          // stencil half width per axis
+  int cell_off;       // first cell of this structure in the global grid
+  int cell_cap;       // atom slots per cell
+  int slot_off;       // first slot of this structure's cells
+  int atom_off, natoms;
+};
+
+// ----------------------------------------------------------------------
+// launchers (defined in the .cu files)
+// ----------------------------------------------------------------------
+struct NbBuffers {
+  const StructGeom* geom;
+  const int* atom_struct;     // [N]
+  double* s_wrap;             // [N][3] wrapped lattice coordinates
+  double* r_wrap;             // [N][3] Cartesian of the wrapped coordinates
+  float4* r_f32;              // [N] (x, y, z, species as int bits)
+  int* cell_of;               // [N] packed cell coordinates cx|cy<<10|cz<<20
+  int* cell_count;            // [ncells_total]
+  int* cell_atoms;            // [nslots]
+  int ncells_total;
+  int nstruc;
+  int cap;                    // neighbour slots per atom
+  int* nb_cnt;
+  int* nb_jt;
+  void* nb_vec;               // float4 or double4_32a
+  int* nb_img;                // optional: image T packed 3 x 10-bit signed
+  unsigned* status;
+};
+
+int ae_launch_neighbors(int natoms, const double* pos, const int* types,
+                        const NbBuffers& nb, int fp64, cudaStream_t s);
+
+struct DescBuffers {
+  int natoms;
+  const int* types;
+  const int* nb_cnt;
+  const int* nb_jt;
+  const void* nb_vec;
+  int cap;
+  void* G;                     // [N][nsf_pad] (T)
+  void* dEdG;                  // [N][nsf_pad] (T)
+  double* E_atom;              // [N]
+  void* F;                     // [N][4] (T) force accumulator (T=float: float4)
+  double* virial;             // [nstruc][9] or null
+  const int* atom_struct;
+  const double* grad_scale;    // per structure factor on dE (or null = 1)
+  unsigned* status;
+};
+
+int ae_launch_chebyshev_forward(const PotDevice& pd, const DescBuffers& b,
+                                int fp64, cudaStream_t s);
+int ae_launch_chebyshev_adjoint(const PotDevice& pd, const DescBuffers& b,
+                                int fp64, cudaStream_t s);
+int ae_launch_behler_forward(const PotDevice& pd, const DescBuffers& b,
+                             int fp64, cudaStream_t s);
+int ae_launch_behler_adjoint(const PotDevice& pd, const DescBuffers& b,
+                             int fp64, cudaStream_t s);
+int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64,
+                  cudaStream_t s);
+int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes,
+                    unsigned* status, cudaStream_t s);
+int ae_launch_energy_reduce(int nstruc, const StructGeom* geom,
+                            const double* E_atom, double* E_struct,
+                            cudaStream_t s);
+int ae_launch_forces_out(int natoms, const void* Facc, int fp64, double* F,
+                         double sign, cudaStream_t s);

@@ -1,0 +1,247 @@
+// Per-species feed-forward networks: energy and dE/dG (replaces ff_eval /
+// ff_deriv of src/ext/feedforward.f90:586-757 and the energy assembly of
+// src/aenet.f90:464-469), plus the per-structure energy reduction and the
+// force output conversion.
+//
+// Weights of every species are staged once per block in shared memory;
+// blocks are persistent (grid-stride over atoms), one warp per atom, lane o
+// computing node o of a layer.  Rows of a layer's weight matrix are stored
+// W[o][k] with the bias in column n_in and an odd row pitch, so that both
+// the forward pass (lanes over rows) and the backward pass (lanes over
+// columns) read shared memory without bank conflicts.
+//
+// dE/dG is written already multiplied by E_scale and by the descriptor
+// normalisation scale 1/s (sfsetup.f90:1010-1031): the adjoint kernels
+// contract it with the derivatives of the raw descriptor.
+#include "common.h"
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  return v;
+}
+
+__device__ __forceinline__ float tanh_t(float x) { return tanhf(x); }
+__device__ __forceinline__ double tanh_t(double x) { return tanh(x); }
+__device__ __forceinline__ float exp_t(float x) { return expf(x); }
+__device__ __forceinline__ double exp_t(double x) { return exp(x); }
+
+// ff_activate: feedforward.f90:932-969
+template <typename T>
+__device__ __forceinline__ void activate(int t, T x, T& y, T& dy) {
+  const T a = T(1.7159), b = T(0.666666666666667), c = T(0.1);
+  switch (t) {
+    case 0: y = x; dy = T(1); break;
+    case 1: y = tanh_t(x); dy = T(1) - y * y; break;
+    case 2: y = T(1) / (T(1) + exp_t(-x)); dy = y * (T(1) - y); break;
+    case 3: { T tb = tanh_t(b * x); y = a * tb; dy = a * (T(1) - tb * tb) * b; } break;
+    case 4: { T tb = tanh_t(b * x); y = a * tb + c * x; dy = a * (T(1) - tb * tb) * b + c; } break;
+    default: y = T(0); dy = T(0);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T nscale(const PotDevice& pd, size_t k);
+template <>
+__device__ __forceinline__ float nscale<float>(const PotDevice& pd, size_t k) { return pd.scale32[k]; }
+template <>
+__device__ __forceinline__ double nscale<double>(const PotDevice& pd, size_t k) { return pd.scale[k]; }
+
+__host__ __device__ constexpr int mlp_warp_elems() {
+  return 2 * (AE_MAXNSF + 1) + 2 * AE_MAXLAYERS * (AE_MAXNODES + 1) + 1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mlp(PotDevice pd, DescBuffers b, const T* __restrict__ W,
+                                             int wtotal) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sW = reinterpret_cast<T*>(smem_raw);
+  const int warps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  for (int q = threadIdx.x; q < wtotal; q += blockDim.x) sW[q] = W[q];
+  // per warp: input features and their gradient (up to AE_MAXNSF), then
+  // activations and derivatives of layers 1 .. L-1 (up to AE_MAXNODES)
+  const int stride = AE_MAXNODES + 1;
+  T* xin = sW + ((wtotal + 1) & ~1) + (size_t)warp * mlp_warp_elems();
+  T* gin = xin + (AE_MAXNSF + 1);
+  T* act = gin + (AE_MAXNSF + 1);
+  T* der = act + AE_MAXLAYERS * stride;
+  __syncthreads();
+
+  for (int i = blockIdx.x * warps + warp; i < b.natoms; i += gridDim.x * warps) {
+    const int ti = b.types[i];
+    const SpeciesTable& sp = pd.sp[ti];
+    const NetTable& net = sp.net;
+    const int nsf = sp.nsf;
+    const T* G = reinterpret_cast<const T*>(b.G) + (size_t)i * pd.nsf_pad;
+    for (int k = lane; k < nsf; k += 32) xin[k] = G[k];
+    __syncwarp();
+    T y = T(0);
+    const int L = net.nlayers;
+    for (int l = 0; l < L - 1; ++l) {
+      const int nin = net.nnodes[l], nout = net.nnodes[l + 1];
+      const T* Wl = sW + net.w_off[l];
+      const int pitch = net.pitch[l];
+      const T* hin = (l == 0) ? xin : act + l * stride;
+      T* hout = act + (l + 1) * stride;
+      T* dout = der + (l + 1) * stride;
+      if (nout == 1) {
+        T part = T(0);
+        for (int k = lane; k < nin; k += 32) part += Wl[k] * hin[k];
+        part = warp_sum(part) + Wl[nin];
+        T yy, dy;
+        activate<T>(net.f_a[l + 1], part, yy, dy);
+        if (lane == 0) {
+          hout[0] = yy;
+          dout[0] = dy;
+        }
+        y = yy;
+      } else {
+        for (int o = lane; o < nout; o += 32) {
+          const T* row = Wl + o * pitch;
+          T z = row[nin];
+          for (int k = 0; k < nin; ++k) z += row[k] * hin[k];
+          T yy, dy;
+          activate<T>(net.f_a[l + 1], z, yy, dy);
+          hout[o] = yy;
+          dout[o] = dy;
+        }
+      }
+      __syncwarp();
+    }
+    // backward: delta of the output node (dE/dy = 1 times f'(z_out)), then
+    // delta_l = (W_l^T delta_{l+1}) * f'_l down to the inputs
+    const T* delta_cur = der + (L - 1) * stride;
+    for (int l = L - 2; l >= 0; --l) {
+      const int nin = net.nnodes[l], nout = net.nnodes[l + 1];
+      const T* Wl = sW + net.w_off[l];
+      const int pitch = net.pitch[l];
+      T* dl = (l == 0) ? gin : der + l * stride;
+      for (int k = lane; k < nin; k += 32) {
+        T s = T(0);
+        for (int o = 0; o < nout; ++o) s += Wl[o * pitch + k] * delta_cur[o];
+        dl[k] = (l > 0) ? s * dl[k] : s;
+      }
+      __syncwarp();
+      delta_cur = dl;
+    }
+    // delta_cur = dE/dG (normalised inputs)
+    T* out = reinterpret_cast<T*>(b.dEdG) + (size_t)i * pd.nsf_pad;
+    const T es = T(sp.E_scale);
+    for (int k = lane; k < nsf; k += 32)
+      out[k] = es * delta_cur[k] * nscale<T>(pd, (size_t)ti * pd.nsf_pad + k);
+    if (lane == 0) b.E_atom[i] = sp.E_scale * (double)y + sp.E_shift + sp.E_atom;
+    __syncwarp();
+  }
+}
+
+// Per-structure energy with Neumaier-compensated FP64 summation: one warp
+// per structure, each lane sums a strided subset, then the (sum,
+// compensation) pairs are combined by a butterfly of two-sums.
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e) {
+  s = a + b;
+  double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__global__ void k_energy_reduce(int nstruc, const StructGeom* geom, const double* __restrict__ E_atom,
+                                double* __restrict__ E_struct) {
+  const int lane = threadIdx.x & 31;
+  const int sidx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (sidx >= nstruc) return;
+  const StructGeom& g = geom[sidx];
+  double s = 0.0, c = 0.0;
+  for (int a = lane; a < g.natoms; a += 32) {
+    double t, e;
+    two_sum(s, E_atom[g.atom_off + a], t, e);
+    s = t;
+    c += e;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    double so = __shfl_xor_sync(0xffffffffu, s, d);
+    double co = __shfl_xor_sync(0xffffffffu, c, d);
+    double t, e;
+    two_sum(s, so, t, e);
+    s = t;
+    c = c + co + e;
+  }
+  if (lane == 0) E_struct[sidx] = s + c;
+}
+
+template <typename T>
+__global__ void k_forces_out(int natoms, const T* __restrict__ Facc, double* __restrict__ F,
+                             double f) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  F[3 * i] = f * (double)Facc[4 * i];
+  F[3 * i + 1] = f * (double)Facc[4 * i + 1];
+  F[3 * i + 2] = f * (double)Facc[4 * i + 2];
+}
+
+__global__ void k_types(int natoms, const int* __restrict__ t1, int* __restrict__ t0, int ntypes,
+                        unsigned* status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  int t = t1[i] - 1;
+  if (t < 0 || t >= ntypes) {
+    atomicOr(status, AE_ST_BAD_TYPE);
+    t = 0;
+  }
+  t0[i] = t;
+}
+
+}  // namespace
+
+int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes, unsigned* status,
+                    cudaStream_t s) {
+  if (natoms <= 0) return 0;
+  k_types<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, types1, types0, ntypes, status);
+  return (int)cudaGetLastError();
+}
+
+int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStream_t s) {
+  if (b.natoms <= 0) return 0;
+  int wtotal = 0;
+  for (int t = 0; t < pd.ntypes; ++t) wtotal = max(wtotal, pd.sp[t].net.wtotal);
+  const int warps = 8;
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const size_t tsz = fp64 ? sizeof(double) : sizeof(float);
+  size_t smem = tsz * (((size_t)wtotal + 1) & ~(size_t)1) + tsz * (size_t)warps * mlp_warp_elems();
+  int blocks = (b.natoms + warps - 1) / warps;
+  int maxb = nsm * 4;
+  if (blocks > maxb) blocks = maxb;
+  if (fp64) {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_mlp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mlp<double><<<blocks, warps * 32, smem, s>>>(pd, b, pd.w64, wtotal);
+  } else {
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_mlp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_mlp<float><<<blocks, warps * 32, smem, s>>>(pd, b, pd.w32, wtotal);
+  }
+  return (int)cudaGetLastError();
+}
+
+int ae_launch_energy_reduce(int nstruc, const StructGeom* geom, const double* E_atom,
+                            double* E_struct, cudaStream_t s) {
+  if (nstruc <= 0) return 0;
+  k_energy_reduce<<<(nstruc + 7) / 8, 256, 0, s>>>(nstruc, geom, E_atom, E_struct);
+  return (int)cudaGetLastError();
+}
+
+int ae_launch_forces_out(int natoms, const void* Facc, int fp64, double* F, double sign,
+                         cudaStream_t s) {
+  if (natoms <= 0) return 0;
+  if (fp64)
+    k_forces_out<double><<<(natoms + 255) / 256, 256, 0, s>>>(natoms, (const double*)Facc, F, sign);
+  else
+    k_forces_out<float><<<(natoms + 255) / 256, 256, 0, s>>>(natoms, (const float*)Facc, F, sign);
+  return (int)cudaGetLastError();
+}

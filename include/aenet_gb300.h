@@ -1,0 +1,140 @@
+/*
+ * aenet_gb300.h -- extensions of the libaenet C API for whole structures
+ * and batches, served by the same library (libaenet_gb300.so) and the same
+ * potential state as aenet.h.
+ *
+ * The reference evaluates one atom per call (src/aenet.f90:410-486) inside
+ * predict.x's per-atom loop (src/predict.F90:574-706), with its own
+ * linked-cell neighbour list (src/ext/lclist.f90).  These entry points take
+ * whole structures instead: the neighbour search, descriptors, networks,
+ * forces, virial and energy reduction all run on the GPU.
+ *
+ * Precision: AENET_GPU_FP64 evaluates everything in FP64 (the plain path,
+ * parity with the reference to 1e-10 eV/atom); AENET_GPU_MIXED evaluates
+ * descriptors, networks and forces in FP32 with the normalisation and the
+ * per-structure energy sums in FP64.
+ *
+ * All arrays are plain C arrays; no function aborts the process.
+ */
+#ifndef AENET_GB300_H_INCLUDED
+#define AENET_GB300_H_INCLUDED
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AENET_GPU_FP64 0
+#define AENET_GPU_MIXED 1
+
+/* additional status codes (the reference's 0..4 keep their meaning) */
+#define AENET_ERR_CUDA 5       /* a CUDA call failed */
+#define AENET_ERR_INPUT 6      /* invalid argument or non-finite coordinate */
+
+/* run flags */
+#define AENET_GPU_FORCES 1u
+#define AENET_GPU_VIRIAL 2u
+
+/* Options of the evaluator.  Keys:
+ *   "angular_domain" = "current" | "legacy"
+ *       current: T_n(cos theta) (src/ext/sfbasis.f90:825, 832);
+ *       legacy : T_n((2 cos theta - pi)/pi), the mapping the Chebyshev
+ *                potentials shipped with aenet were trained with.
+ *   "cell_div" = "1" | "2" | "3"   cells per cut-off length in the
+ *       neighbour search grid (performance only).
+ * Returns AENET_OK or AENET_ERR_INPUT.  Takes effect at the next load or
+ * plan creation. */
+int aenet_gpu_set_option(const char* key, const char* value);
+
+/* Energy and forces of one structure from HOST arrays.  Replaces the atom
+ * loop of predict.x's get_energy (src/predict.F90:574-706): coords[3*natoms]
+ * Cartesian, type_ids[natoms] 1-based, lattice[9] rows = lattice vectors
+ * (ignored when pbc == 0: an isolated structure), precision
+ * AENET_GPU_FP64 | AENET_GPU_MIXED.  Outputs (any may be NULL): *E_total
+ * (sum of atomic energies including free-atom energies), *E_coh (minus the
+ * free-atom energies), E_atoms[natoms], F[3*natoms] (overwritten),
+ * virial[9] (W_ab = -dE/d(strain_ab), eV). */
+void aenet_gpu_structure_energy_forces(int natoms, const double* coords,
+                                       const int* type_ids,
+                                       const double* lattice, int pbc,
+                                       int precision, double* E_total,
+                                       double* E_coh, double* E_atoms,
+                                       double* F, double* virial, int* stat);
+
+/* Batched evaluation with HOST arrays: nstruc structures packed
+ * back-to-back (natoms[s] atoms each), lattices[9*nstruc], pbc[nstruc].
+ * E[nstruc] total energies, F[3*sum natoms], virial[9*nstruc] (optional). */
+void aenet_gpu_batch_energy_forces(int nstruc, const int* natoms,
+                                   const double* coords, const int* type_ids,
+                                   const double* lattices, const int* pbc,
+                                   int precision, double* E, double* F,
+                                   double* virial, int* stat);
+
+/* ---- device-resident plans (stream ordered, no allocation per run) ----
+ * A plan fixes the batch layout (structure sizes, cells, pbc) and owns the
+ * device workspace.  Runs read positions and write results in DEVICE
+ * memory on the given CUDA stream and may be captured in a CUDA graph. */
+typedef struct aenet_gpu_plan aenet_gpu_plan;
+
+/* coords0 (host, may be NULL for periodic batches) gives the initial
+ * positions used to size the binning boxes of isolated structures. */
+aenet_gpu_plan* aenet_gpu_plan_create(int nstruc, const int* natoms,
+                                      const double* lattices, const int* pbc,
+                                      const double* coords0, int precision,
+                                      int* stat);
+void aenet_gpu_plan_destroy(aenet_gpu_plan* plan);
+int aenet_gpu_plan_natoms(const aenet_gpu_plan* plan);
+/* Replace the lattice of every structure (host array, 9*nstruc); the cell
+ * grids must stay within the capacities chosen at creation. */
+int aenet_gpu_plan_set_lattices(aenet_gpu_plan* plan, const double* lattices);
+
+/* Full pass: neighbours, descriptors, networks, energies and (flags)
+ * forces / virial.  d_coords[3*N] (double), d_types[N] (int, 1-based);
+ * outputs in device memory, any may be NULL: d_E[nstruc], d_E_atoms[N],
+ * d_F[3*N] (double, overwritten), d_virial[9*nstruc]. */
+int aenet_gpu_plan_run(aenet_gpu_plan* plan, const double* d_coords,
+                       const int* d_types, double* d_E, double* d_E_atoms,
+                       double* d_F, double* d_virial, unsigned flags,
+                       void* stream);
+
+/* Split pass for automatic differentiation: forward computes energies and
+ * keeps dE/dG; backward then writes d_grad[3*N] = sum_s w[s] dE_s/dR
+ * (w = d_weights[nstruc], device, NULL = all ones) and optionally the
+ * virial of the weighted energy. */
+int aenet_gpu_plan_forward(aenet_gpu_plan* plan, const double* d_coords,
+                           const int* d_types, double* d_E,
+                           double* d_E_atoms, void* stream);
+int aenet_gpu_plan_backward(aenet_gpu_plan* plan, const double* d_weights,
+                            double* d_grad, double* d_virial, void* stream);
+
+/* The full pass with forces, with CUDA events recorded on `stream` between
+ * the stages; ms[7] receives the stage durations in milliseconds: type
+ * check, neighbour search, descriptor, networks, energy reduction,
+ * adjoint, force output.  Synchronises the stream. */
+int aenet_gpu_plan_profile(aenet_gpu_plan* plan, const double* d_coords,
+                           const int* d_types, double* d_E, double* d_F,
+                           float* ms, void* stream);
+
+/* Device status word of the last run: 0, or AENET_GPU_ST_* bits. */
+#define AENET_GPU_ST_NB_OVERFLOW 1u
+#define AENET_GPU_ST_BAD_COORD 2u
+#define AENET_GPU_ST_BAD_TYPE 4u
+#define AENET_GPU_ST_CELL_OVERFLOW 8u
+unsigned aenet_gpu_plan_status(aenet_gpu_plan* plan, void* stream);
+
+/* Neighbour table of the last run (device pointers, for inspection and
+ * tests): cap slots per atom, counts[N], packed index|species<<26, and
+ * (x, y, z, distance) vectors as double4 (FP64 plans) or float4. */
+int aenet_gpu_plan_neighbors(aenet_gpu_plan* plan, int* cap,
+                             const int** d_counts, const int** d_jt,
+                             const void** d_vec);
+
+/* Descriptor of the last forward (device, [N][nsf_pad], double for FP64
+ * plans, float for mixed) and its row stride. */
+int aenet_gpu_plan_descriptors(aenet_gpu_plan* plan, const void** d_G,
+                               int* nsf_pad);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -203,12 +203,13 @@ class Oracle:
         self.lib.orc_cart_to_latt(_f64(cell), cart.shape[0], cart, out)
         return out
 
-    def neighbors(self, cell, cart, types, pbc=True, Rc=None):
+    def neighbors(self, cell, cart, types, pbc=True, Rc=None, atoms=None):
         """Per-atom neighbour lists of lcl_nbdist_cart (predict.x order).
 
         Returns the wrapped lattice coordinates, the Cartesian centre
         positions and a list of (nbcoo, nbdist, nblist, nbtype) per atom
-        (nblist 1-based).
+        (nblist 1-based).  ``atoms`` (0-based ids) restricts the queries;
+        the list then holds entries only for those atoms, in that order.
         """
         cart = _f64(cart).copy()
         cell = _f64(cell)
@@ -224,7 +225,8 @@ class Oracle:
         Rc = self.Rc_max if Rc is None else Rc
         cap = max(self.nnb_max, 64)
         out = []
-        for i in range(1, n + 1):
+        for i in ((np.arange(n) + 1) if atoms is None else (np.asarray(atoms) + 1)):
+            i = int(i)
             while True:
                 nbcoo = np.zeros((cap, 3)); nbdist = np.zeros(cap)
                 nbl = np.zeros(cap, dtype=np.int32); nbt = np.zeros(cap, dtype=np.int32)

@@ -1,0 +1,344 @@
+"""GPU evaluator against the FP64 oracle and the reference's golden values.
+
+Tolerances (stated by the evaluation contract):
+  FP64 path   energy within 1e-10 eV/atom of the oracle, forces 1e-9 eV/A;
+              neighbour sets identical (bit for bit).
+  mixed path  energy within 1 meV/atom, force RMS within 20 meV/A of FP64.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tests import helpers
+from tests.golden import fixtures
+
+pytestmark = pytest.mark.gpu
+
+E_TOL_FP64 = 1e-10      # eV/atom
+F_TOL_FP64 = 1e-9       # eV/A
+E_TOL_MIXED = 1e-3      # eV/atom
+F_RMS_MIXED = 2e-2      # eV/A
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def cu256(oracle, tmp_path_factory):
+    from aenet_gb300 import workloads
+    w = workloads.cu_fcc_256()
+    d = tmp_path_factory.mktemp("cu256")
+    oracle.set_candidates("cells")
+    paths = helpers.make_potentials(oracle, w, str(d))
+    oracle.set_candidates("complete")
+    return w, paths
+
+
+@pytest.fixture(scope="module")
+def aucu(oracle, tmp_path_factory):
+    from aenet_gb300 import workloads
+    w = workloads.aucu_fcc_4000()
+    d = tmp_path_factory.mktemp("aucu")
+    paths = helpers.make_potentials(oracle, w, str(d), max_atoms=1000)
+    return w, paths
+
+
+def _ann(paths, types, angular=None):
+    from aenet_gb300.core import ANNPotentials
+    return ANNPotentials({t: paths[t] for t in types}, angular_domain=angular or "current")
+
+
+def test_k1_ti2o4_golden_energy_on_gpu(cuda, oracle, tmp_path):
+    from aenet_gb300.core import FP64
+    k1 = fixtures.load("k1_ti2o4.npz")
+    pots = fixtures.potentials(k1)
+    paths = fixtures.write_potential_files(pots, str(tmp_path))
+    sym = [str(s) for s in k1["symbols"]]
+    ann = _ann(paths, ["Ti", "O"], "legacy")
+    try:
+        r = ann.structure_energy_forces(k1["positions"], sym, k1["cell"], precision=FP64)
+        assert ann.Rc_min == 0.55 and ann.Rc_max == 8.0
+    finally:
+        ann.release()
+    assert abs(r["energy"] - float(k1["E_total"])) < 1e-9
+    oracle.load(["Ti", "O"], pots, angular="legacy")
+    types = np.array([1 if s == "Ti" else 2 for s in sym], dtype=np.int32)
+    ec, et, F, Ea = oracle.structure(k1["cell"], k1["positions"], types)
+    assert np.abs(r["forces"] - F).max() < F_TOL_FP64
+    assert np.abs(r["atomic_energies"] - Ea).max() < E_TOL_FP64
+    assert abs(r["cohesive_energy"] - ec) < 1e-9
+
+
+def test_cu256_fp64_matches_oracle(cuda, oracle, cu256):
+    from aenet_gb300.core import FP64
+    w, paths = cu256
+    s = w.structures[0]
+    ann = _ann(paths, w.types)
+    try:
+        r = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64, virial=True)
+    finally:
+        ann.release()
+    oracle.load(w.types, paths)
+    ec, et, F, Ea = oracle.structure(s.cell, s.positions, s.types)
+    n = s.natoms
+    assert abs(r["energy"] - et) / n < E_TOL_FP64
+    assert np.abs(r["atomic_energies"] - Ea).max() < E_TOL_FP64
+    assert np.abs(r["forces"] - F).max() < F_TOL_FP64
+    assert np.abs(r["forces"].sum(0)).max() < 1e-9
+
+
+def test_cu256_virial_matches_strain_derivative(cuda, oracle, cu256):
+    """W = -dE/d(strain) by central differences of the oracle energy."""
+    from aenet_gb300.core import FP64
+    w, paths = cu256
+    s = w.structures[0]
+    ann = _ann(paths, w.types)
+    try:
+        r = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64, virial=True)
+    finally:
+        ann.release()
+    oracle.load(w.types, paths)
+    h = 1e-5
+    W = np.zeros((3, 3))
+    for a in range(3):
+        for b in range(3):
+            E = []
+            for sgn in (-1, 1):
+                eps = np.eye(3)
+                eps[a, b] += sgn * h
+                E.append(oracle.structure(s.cell @ eps, s.positions @ eps, s.types,
+                                          forces=False)[1])
+            W[a, b] = -(E[1] - E[0]) / (2 * h)
+    assert np.abs(r["virial"] - W).max() < 1e-5 * max(1.0, np.abs(W).max())
+
+
+def test_neighbour_sets_bit_exact(cuda, oracle, cu256):
+    """aenet_nbl_* against the oracle's complete lcl_nbdist_cart lists on the
+    same lattice coordinates: identical (atom, image) sets and coordinates."""
+    from aenet_gb300 import _lib, workloads
+    lib = _lib.lib()
+    w, paths = cu256
+    rng = np.random.default_rng(7)
+    cases = [(w.structures[0].cell, w.structures[0].positions, w.structures[0].types)]
+    k1 = fixtures.load("k1_ti2o4.npz")
+    cases.append((k1["cell"], k1["positions"], np.array([1, 1, 1, 1, 1, 1], dtype=np.int32)))
+    for n in (16, 40, 120):      # cells shorter than the cut-off: many images
+        pos, cell = workloads.random_cell(rng, n)
+        cases.append((cell, pos, np.ones(n, dtype=np.int32)))
+    tric = np.array([[5.1, 0.0, 0.0], [1.7, 4.9, 0.0], [-1.2, 0.8, 6.3]])
+    cases.append((tric, rng.uniform(0, 5, (30, 3)), np.ones(30, dtype=np.int32)))
+    ann = _ann(paths, w.types)
+    oracle.load(w.types, paths)
+    try:
+        for cell, pos, types in cases:
+            latt, centres, ref = oracle.neighbors(cell, pos, types)
+            # give the GPU the same lattice coordinates (cartesian = False)
+            s_in = oracle.cart_to_latt(np.ascontiguousarray(cell, dtype=np.float64), pos)
+            coords = np.ascontiguousarray(s_in.copy())
+            L = np.ascontiguousarray(cell, dtype=np.float64)
+            tt = np.ascontiguousarray(types, dtype=np.int32)
+            lib.aenet_nbl_init(L.ctypes.data_as(C.c_void_p), len(pos),
+                               tt.ctypes.data_as(C.c_void_p), coords.ctypes.data_as(C.c_void_p),
+                               False, True)
+            for i in range(len(pos)):
+                cap = 4096
+                nnb = C.c_int(cap)
+                nbcoo = np.zeros((cap, 3))
+                nbdist = np.zeros(cap)
+                nbl = np.zeros(cap, dtype=np.int32)
+                nbt = np.zeros(cap, dtype=np.int32)
+                lib.aenet_nbl_neighbors(i + 1, C.byref(nnb), nbcoo.ctypes.data_as(C.c_void_p),
+                                        nbdist.ctypes.data_as(C.c_void_p),
+                                        nbl.ctypes.data_as(C.c_void_p),
+                                        nbt.ctypes.data_as(C.c_void_p))
+                k = nnb.value
+                got = sorted(zip(nbl[:k].tolist(), map(tuple, nbcoo[:k].tolist())))
+                rc, _, rl, _ = ref[i]
+                exp = sorted(zip(rl.tolist(), map(tuple, rc.tolist())))
+                assert len(got) == len(exp), (i, len(got), len(exp))
+                assert got == exp
+            np.testing.assert_allclose(coords, latt @ L, rtol=0, atol=1e-12)
+            lib.aenet_nbl_final()
+    finally:
+        ann.release()
+
+
+def test_per_atom_api_matches_oracle(cuda, oracle, cu256):
+    """aenet_atomic_energy(_and_forces) with caller-supplied neighbours."""
+    w, paths = cu256
+    s = w.structures[0]
+    oracle.load(w.types, paths)
+    _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types)
+    ann = _ann(paths, w.types)
+    try:
+        F_gpu = np.zeros((s.natoms, 3))
+        F_or = np.zeros((s.natoms, 3))
+        for i in (0, 17, 255):
+            nbcoo, _, nbl, nbt = nb[i]
+            sym = [w.types[t - 1] for t in nbt]
+            e_gpu = ann.atomic_energy_and_forces(centres[i], w.types[s.types[i] - 1], i + 1,
+                                                 nbcoo, sym, nbl, F_gpu)
+            e_or = oracle.atomic_energy_and_forces(centres[i], int(s.types[i]), i + 1, nbcoo,
+                                                   nbt, nbl, F_or)
+            assert abs(e_gpu - e_or) < E_TOL_FP64
+            e2 = ann.atomic_energy(centres[i], w.types[s.types[i] - 1], nbcoo, sym)
+            assert abs(e2 - e_or) < E_TOL_FP64
+        assert np.abs(F_gpu - F_or).max() < F_TOL_FP64
+    finally:
+        ann.release()
+
+
+def test_aucu4000_mixed_vs_fp64(cuda, oracle, aucu):
+    from aenet_gb300.core import FP64, MIXED
+    w, paths = aucu
+    s = w.structures[0]
+    ann = _ann(paths, w.types)
+    try:
+        r64 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64)
+        r32 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=MIXED)
+    finally:
+        ann.release()
+    oracle.load(w.types, paths)
+    oracle.set_candidates("cells")
+    try:
+        ec, et, F, Ea = oracle.structure(s.cell, s.positions, s.types, nthreads=8)
+    finally:
+        oracle.set_candidates("complete")
+    n = s.natoms
+    assert abs(r64["energy"] - et) / n < E_TOL_FP64
+    assert np.abs(r64["forces"] - F).max() < F_TOL_FP64
+    dE = abs(r32["energy"] - r64["energy"]) / n
+    dF = r32["forces"] - r64["forces"]
+    assert dE < E_TOL_MIXED, dE
+    assert np.sqrt(np.mean(dF ** 2)) < F_RMS_MIXED
+    assert np.abs(dF).max() < 10 * F_RMS_MIXED
+
+
+def test_autograd_adjoint_and_finite_differences(cuda, aucu):
+    """Forces from torch.autograd through the adjoint kernels: equal to the
+    plan's forces, and to central differences (h = 1e-4 A) on 64 atoms."""
+    torch = cuda
+    from aenet_gb300.core import FP64, MIXED
+    from aenet_gb300.plan import Plan, potential_energy
+    w, paths = aucu
+    s = w.structures[0]
+    ann = _ann(paths, w.types)
+    try:
+        for prec, tol in ((FP64, 1e-6), (MIXED, 3e-2)):
+            plan = Plan([s.natoms], [s.cell], precision=prec)
+            pos = torch.tensor(s.positions, device="cuda", requires_grad=True)
+            types = torch.tensor(s.types, device="cuda", dtype=torch.int32)
+            E = potential_energy(pos, plan, types)
+            E.sum().backward()
+            grad = pos.grad.clone()
+            out = plan.run(pos.detach(), types, forces=True)
+            torch.testing.assert_close(grad, -out["F"], rtol=0, atol=1e-12)
+            rng = np.random.default_rng(11)
+            atoms = rng.choice(s.natoms, 64, replace=False)
+            h = 1e-4
+            p0 = pos.detach().clone()
+
+            def central(a, c, hh):
+                pp = p0.clone(); pp[a, c] += hh
+                pm = p0.clone(); pm[a, c] -= hh
+                return (plan.forward(pp, types)[0].item()
+                        - plan.forward(pm, types)[0].item()) / (2 * hh)
+
+            for a in atoms[:16 if prec == MIXED else 64]:
+                c = int(rng.integers(3))
+                if prec == FP64:
+                    # Richardson extrapolation removes the O(h^2) term
+                    fd = (4 * central(a, c, h / 2) - central(a, c, h)) / 3
+                else:
+                    fd = central(a, c, h)
+                assert abs(fd - grad[a, c].item()) < tol, (prec, a, c, fd, grad[a, c].item())
+            plan.close()
+    finally:
+        ann.release()
+
+
+def test_batch_of_small_cells_matches_oracle(cuda, oracle, tmp_path):
+    """Several small periodic cells (cut-off longer than the cell: many
+    images) in one batched call, FP64 against the oracle per structure."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64
+    w = workloads.lisio_batch_4096(nstruc=6)
+    oracle.set_candidates("cells")
+    paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    oracle.set_candidates("complete")
+    ann = _ann(paths, w.types)
+    try:
+        structs = [(s.positions, s.types, s.cell, True) for s in w.structures]
+        r = ann.batch_energy_forces(structs, precision=FP64)
+    finally:
+        ann.release()
+    oracle.load(w.types, paths)
+    off = 0
+    for k, s in enumerate(w.structures):
+        ec, et, F, _ = oracle.structure(s.cell, s.positions, s.types)
+        assert abs(r["energy"][k] - et) / s.natoms < E_TOL_FP64
+        assert np.abs(r["forces"][off:off + s.natoms] - F).max() < F_TOL_FP64
+        off += s.natoms
+
+
+def test_sfb_api_matches_oracle(cuda, oracle):
+    from aenet_gb300 import _lib
+    lib = _lib.lib()
+    names = (C.c_char_p * 2)(b"Au", b"Cu")
+    st = C.c_int(-1)
+    lib.aenet_sfb_init(2, names, 12, 6, 6.5, 4.5, C.byref(st))
+    assert st.value == 0
+    try:
+        nv = lib.aenet_sfb_nvalues()
+        assert nv == 40
+        rng = np.random.default_rng(3)
+        coo1 = rng.uniform(-4, 4, (30, 3))
+        it = rng.integers(1, 3, 30).astype(np.int32)
+        coo0 = np.zeros(3)
+        vals = np.zeros(nv)
+        lib.aenet_sfb_eval(1, coo0.ctypes.data_as(C.c_void_p), 30, it.ctypes.data_as(C.c_void_p),
+                           coo1.ctypes.data_as(C.c_void_p), nv, vals.ctypes.data_as(C.c_void_p),
+                           C.byref(st))
+        assert st.value == 0
+        olib = oracle.lib
+        olib.orc_sfb_init(2, 12, 6, 6.5, 4.5)
+        ref = np.zeros(nv)
+        olib.orc_sfb_eval(1, coo0, 30, it, np.ascontiguousarray(coo1), nv, ref, None, None)
+        olib.orc_sfb_final()
+        np.testing.assert_allclose(vals, ref, rtol=0, atol=1e-11)
+    finally:
+        lib.aenet_sfb_final(C.byref(st))
+
+
+def test_capacity_overflow_is_reported_and_retried(cuda, cu256):
+    torch = cuda
+    from aenet_gb300.core import FP64
+    from aenet_gb300.plan import Plan, PlanStatusError
+    w, paths = cu256
+    s = w.structures[0]
+    ann = _ann(paths, w.types)
+    try:
+        plan = Plan([s.natoms], [s.cell], precision=FP64)
+        pos = torch.tensor(s.positions, device="cuda")
+        types = torch.tensor(s.types, device="cuda", dtype=torch.int32)
+        plan.run(pos, types)
+        plan.check()
+        # squeeze the structure to 60% volume: more neighbours than the
+        # capacity sized for the original density
+        dense = torch.tensor(s.positions * 0.6, device="cuda")
+        plan.set_cells([s.cell * 0.6])
+        plan.run(dense, types)
+        with pytest.raises(PlanStatusError):
+            plan.check()
+        plan.close()
+        # the host-buffer entry point resizes and retries on its own
+        r = ann.structure_energy_forces(s.positions * 0.6, s.types, s.cell * 0.6, precision=FP64)
+        assert np.isfinite(r["energy"])
+    finally:
+        ann.release()
