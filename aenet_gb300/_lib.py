@@ -82,6 +82,8 @@ def _declare(lib):
     lib.aenet_gpu_plan_backward.restype = C.c_int
     lib.aenet_gpu_plan_profile.argtypes = [vp, vp, vp, vp, vp, C.POINTER(C.c_float), vp]
     lib.aenet_gpu_plan_profile.restype = C.c_int
+    lib.aenet_gpu_measure_fp32_peak.argtypes = [dp, vp]
+    lib.aenet_gpu_measure_fp32_peak.restype = C.c_int
     lib.aenet_gpu_plan_status.argtypes = [vp, vp]
     lib.aenet_gpu_plan_status.restype = C.c_uint
     lib.aenet_gpu_plan_neighbors.argtypes = [vp, ip, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]

@@ -1708,6 +1708,12 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   return e ? AENET_ERR_CUDA : 0;
 }
 
+EXPORT int aenet_gpu_measure_fp32_peak(double* tflops, void* stream) {
+  if (!tflops) return AENET_ERR_INPUT;
+  if (!cuda_ok()) return AENET_ERR_CUDA;
+  return ae_fma_peak(tflops, (cudaStream_t)stream) ? AENET_ERR_CUDA : 0;
+}
+
 EXPORT unsigned aenet_gpu_plan_status(aenet_gpu_plan* P, void* stream) {
   if (!P) return 0;
   unsigned v = 0;

@@ -177,6 +177,7 @@ int ae_launch_behler_adjoint(const PotDevice& pd, const DescBuffers& b,
                              int fp64, cudaStream_t s);
 int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64,
                   cudaStream_t s);
+int ae_fma_peak(double* tflops, cudaStream_t s);
 int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes,
                     unsigned* status, cudaStream_t s);
 int ae_launch_energy_reduce(int nstruc, const StructGeom* geom,

@@ -195,7 +195,54 @@ __global__ void k_types(int natoms, const int* __restrict__ t1, int* __restrict_
   t0[i] = t;
 }
 
+// FP32 FMA throughput probe: independent FMA chains per thread, enough
+// blocks to fill every SM.  Used only to measure the denominator of the
+// FP32 roofline of the descriptor kernels.
+__global__ void k_fma_peak(float* out, int iters, float seed) {
+  float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+  float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+  const float m = 0.999999f, c = 1e-7f;
+  for (int k = 0; k < iters; ++k) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+      a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+    }
+  }
+  float r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (r == 12345.678f) out[blockIdx.x] = r;
+}
+
 }  // namespace
+
+int ae_fma_peak(double* tflops, cudaStream_t s) {
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  float* out = nullptr;
+  if (cudaMalloc(&out, 4096 * sizeof(float)) != cudaSuccess) return 1;
+  const int blocks = nsm * 8, threads = 256, iters = 4096;
+  k_fma_peak<<<blocks, threads, 0, s>>>(out, 16, 1.f);   // warm-up
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0, s);
+    k_fma_peak<<<blocks, threads, 0, s>>>(out, iters, 1.f);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return (int)cudaGetLastError();
+}
 
 int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes, unsigned* status,
                     cudaStream_t s) {

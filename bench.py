@@ -1,0 +1,483 @@
+"""Benchmark: atoms/s of energy + forces on one GB300.
+
+Workload (the batched configuration the metric is quoted on): 4096 cubic
+Li/Si/O cells with log-uniform atom counts in [16, 512] (~597k atoms),
+Chebyshev descriptor radial order 10 (Rc 6.0) / angular order 4 (Rc 4.0),
+species-weighted (32 features), one 32-32-32-1 tanh network per species,
+random weights; synthetic data generated from a fixed seed.
+
+A step is one full energy-and-force pass over the whole batch: neighbour
+search, descriptors, networks, energies, adjoint forces.  The batched
+mixed-precision path is timed (the headline) next to the plain FP64 path on
+the same batch; the mixed-precision error against FP64 is reported.
+
+Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events
+on the launching stream, with an L2 flush (a 512 MB write) between steps
+outside the events; barrier + synchronize around the timed region; max over
+ranks.  `e2e` repeats the measurement through the C-ABI host-buffer entry
+point (aenet_gpu_batch_energy_forces) from pinned host memory, copies
+included.  `cpu_baseline` times the FP64 oracle (a restatement of the
+reference's predict.x loop, its linked-cell search included) on a bounded
+sample on all host cores.
+
+--impl reference times that CPU implementation instead (rank 0 only).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "atoms/s E+F on 1 GB300: batched mixed-prec vs plain FP64 at ≤1 meV/atom"
+WORKLOAD = ("lisio_batch_4096: 4096 cubic Li/Si/O cells, 16-512 atoms (log-uniform), "
+            "0.08 atoms/A^3, Chebyshev r10/6.0 a4/4.0 (32 features), 32-32-32-1 x3, E+F")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nstruc", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "aenet_gb300_bench"))
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- workload
+def load_workload(args, rank):
+    """The seeded batch; cached (structures and network weights) on disk
+    because the random placement takes a few seconds."""
+    from aenet_gb300 import nnfile, workloads
+    seed = args.seed + 1000 * rank
+    os.makedirs(args.cache, exist_ok=True)
+    f = os.path.join(args.cache, "lisio_%d_%d.npz" % (seed, args.nstruc))
+    if os.path.exists(f):
+        z = np.load(f)
+        nat = z["natoms"]
+        offs = np.concatenate([[0], np.cumsum(nat)])
+        structs = [workloads.Structure(z["pos"][offs[k]:offs[k + 1]],
+                                       z["typ"][offs[k]:offs[k + 1]], z["cells"][k])
+                   for k in range(len(nat))]
+        types = ["Li", "Si", "O"]
+        arch = [32, 32, 32, 1]
+        w = workloads.Workload("lisio_batch_4096", types,
+                               workloads.cheb_setups(types, 10, 6.0, 4, 4.0), arch, structs, seed)
+        w.networks = {t: nnfile.make_network(arch, z["W_" + t]) for t in types}
+        return w
+    w = workloads.lisio_batch_4096(seed=seed, nstruc=args.nstruc)
+    nat, pos, typ, cells, _ = w.packed()
+    tmp = f + ".tmp%d.npz" % os.getpid()
+    np.savez(tmp, natoms=nat, pos=pos, typ=typ, cells=cells,
+             **{"W_" + t: w.networks[t]["W"] for t in w.types})
+    os.replace(tmp, f)
+    return w
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 8]
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[4 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ----------------------------------------------------------------- helpers
+def neighbour_stats(plan, a_rc, r_rc):
+    import torch
+    cap, cnt, jt, vec = plan.neighbors()
+    d = vec[..., 3]
+    valid = torch.arange(cap, device=d.device)[None, :] < cnt[:, None].long()
+    nr = ((d <= r_rc) & (d > 1e-12) & valid).sum(1).double()
+    na = ((d <= a_rc) & (d >= 1e-12) & valid).sum(1).double()
+    P = na * (na - 1) / 2
+    return {"n_r": nr.mean().item(), "n_a": na.mean().item(), "P": P.mean().item(),
+            "cap": cap, "n_max": int(cnt.max().item())}
+
+
+def cheb_flops(nb, R, A, nsf, m, arch):
+    """Canonical per-atom flop counts of the survey's measurement section."""
+    nr, na, P = nb["n_r"], nb["n_a"], nb["P"]
+    fwd = nr * (16 + (5 + 2 * (m - 1)) * R) + 6 * na + P * (9 + (5 + 2 * (m - 1)) * A) + 2 * nsf
+    adj = nr * (12 + (9 + 2 * (m - 1)) * R) + P * (77 + (8 + 2 * (m - 1)) * A)
+    mlp_f = sum(2 * arch[l] * arch[l + 1] + arch[l + 1] for l in range(len(arch) - 1))
+    mlp_b = sum(2 * arch[l] * arch[l + 1] + 2 * arch[l + 1] for l in range(len(arch) - 1))
+    return {"descriptor": fwd, "adjoint": adj, "networks": mlp_f + mlp_b}
+
+
+def oracle_descriptor_fn(oracle):
+    def fn(workload, paths, ids):
+        oracle.load(workload.types, paths)
+        rows, spec = [], []
+        ids = set(int(i) for i in ids)
+        off = 0
+        for s in workload.structures:
+            local = [i - off for i in range(off, off + s.natoms) if i in ids]
+            off += s.natoms
+            if not local:
+                continue
+            _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types, atoms=local)
+            for q, a in enumerate(local):
+                rows.append(oracle.descriptor(centres[a], int(s.types[a]), nb[q][0], nb[q][3],
+                                              scaled=False))
+                spec.append(int(s.types[a]))
+        return np.array(rows), np.array(spec)
+    return fn
+
+
+def time_oracle(oracle, structures, threads):
+    t0 = time.perf_counter()
+    n = 0
+    for s in structures:
+        oracle.structure(s.cell, s.positions, s.types, nthreads=threads)
+        n += s.natoms
+    return n, time.perf_counter() - t0
+
+
+def pick_sample(oracle, structures, threads, seconds):
+    """Leading structures of the batch whose oracle time is about `seconds`."""
+    probe = structures[:8]
+    n, dt = time_oracle(oracle, probe, threads)
+    per_atom = dt / max(n, 1)
+    budget = seconds / max(per_atom, 1e-9)
+    out, tot = [], 0
+    for s in structures:
+        if tot + s.natoms > budget and out:
+            break
+        out.append(s)
+        tot += s.natoms
+    return out
+
+
+# ----------------------------------------------------------------- arms
+def run_reference(args):
+    """The reference's CPU algorithm (oracle port) on the host cores."""
+    from oracle import Oracle
+    from aenet_gb300 import workloads
+    w = load_workload(args, 0)
+    d = tempfile.mkdtemp(prefix="aenet_ref_")
+    o = Oracle()
+    paths = workloads.write_potentials(w, d, oracle_descriptor_fn(o), max_atoms_for_stats=4000)
+    o.load(w.types, paths)
+    o.set_candidates("cells")
+    threads = os.cpu_count() or 1
+    per_step = max(2.0, args.cpu_seconds * 4 / max(args.steps + args.warmup, 1))
+    sample = pick_sample(o, w.structures, threads, per_step)
+    for _ in range(args.warmup):
+        time_oracle(o, sample, threads)
+    times, atoms = [], 0
+    for _ in range(args.steps):
+        n, dt = time_oracle(o, sample, threads)
+        times.append(dt)
+        atoms = n
+    ms = 1e3 * float(np.mean(times))
+    value = atoms / (ms * 1e-3)
+    desc = ("first %d of %d cells (%d atoms) per step, FP64 oracle port of predict.x "
+            "(linked-cell search as written), %d OpenMP threads" % (len(sample), len(w.structures),
+                                                                     atoms, threads))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atoms/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "sample": desc, "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from aenet_gb300 import _lib, workloads
+    from aenet_gb300.core import ANNPotentials, FP64, MIXED
+    from aenet_gb300.plan import Plan
+
+    w = load_workload(args, rank)
+    d = tempfile.mkdtemp(prefix="aenet_bench_")
+    paths = workloads.write_potentials(w, d, workloads.gpu_descriptor_fn)
+    ann = ANNPotentials(paths)
+    nat, pos, typ, cells, pbc = w.packed()
+    N, S = int(nat.sum()), len(nat)
+    dev = torch.device("cuda", local)
+    p = torch.tensor(pos, device=dev)
+    t = torch.tensor(typ, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    def timed(plan, out, steps, graph):
+        fn = (lambda: graph.replay()) if graph is not None else (lambda: plan.run(p, t, out=out))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        barrier()
+        wall0 = time.perf_counter()
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            fn()
+            ev[k][1].record(stream)
+        barrier()
+        wall = time.perf_counter() - wall0
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return float(np.sum(ms)), wall
+
+    def prepare(prec):
+        plan = Plan(nat, cells, pbc, precision=prec, coords0=pos)
+        out = plan.run(p, t)
+        plan.check()
+        for _ in range(args.warmup):
+            plan.run(p, t, out=out)
+        torch.cuda.synchronize()
+        graph = None
+        if not args.no_graph:
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                plan.run(p, t, out=out)
+            for _ in range(max(1, args.warmup)):
+                graph.replay()
+            torch.cuda.synchronize()
+        return plan, out, graph
+
+    # ---- mixed precision (headline)
+    plan32, out32, g32 = prepare(MIXED)
+    sampler = ClockSampler(local)
+    sampler.start()
+    total_ms, wall = timed(plan32, out32, args.steps, g32)
+    clocks = sampler.stop()
+    plan32.check()
+    tmax = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    total_ms = float(tmax.item())
+    ms_step = total_ms / args.steps
+    value = world * N / (ms_step * 1e-3)
+    res32 = {k: v.clone() for k, v in out32.items()}
+
+    # ---- stage profile and roofline of the dominant kernel
+    stages = {}
+    for _ in range(3):
+        prof = plan32.profile(p, t)
+        for k, v in prof.items():
+            stages[k] = stages.get(k, 0.0) + v / 3
+    sp = w.setups["Li"]
+    r_rc, r_ord, a_rc, a_ord = sp["sfparam"][0]
+    nb = neighbour_stats(plan32, a_rc, r_rc)
+    R, A = int(r_ord) + 1, int(a_ord) + 1
+    fl = cheb_flops(nb, R, A, sp["nsf"], 2, w.arch)
+    peak = C.c_double(0.0)
+    _lib.lib().aenet_gpu_measure_fp32_peak(C.byref(peak), C.c_void_p(stream.cuda_stream))
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
+    kernels = {"descriptor": "k_cheb_forward", "adjoint": "k_cheb_adjoint",
+               "networks": "k_mlp", "neighbours": "k_neighbors"}
+    dom = max(kernels, key=lambda k: stages.get(k, 0.0))
+    cap = nb["cap"]
+    # algorithmic bytes per atom of each kernel (neighbour table at 20 B per
+    # pair: float4 vector + packed index; descriptor rows 4 B per feature)
+    nsf = sp["nsf"]
+    nbytes = {"descriptor": nb["n_r"] * 20 + nsf * 4,
+              "adjoint": nb["n_r"] * 20 + nsf * 4 + 16 * (nb["n_r"] + 1),
+              "networks": 2 * nsf * 4 + 8,
+              "neighbours": 24 + nb["n_r"] * 20 + 16 * 27}
+    dom_ms = stages[dom]
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_per_atom.json")
+    if os.path.exists(tf):
+        per_atom = json.load(open(tf)).get(kernels[dom])
+        traffic = None if per_atom is None else per_atom * N
+    if dom in ("descriptor", "adjoint", "networks"):
+        ach = fl[dom] * N / (dom_ms * 1e-3) / 1e12
+        roof = {"bound": "fp32", "kernel": kernels[dom], "achieved": ach, "peak": peak.value,
+                "unit": "TFLOP/s", "frac": ach / peak.value if peak.value else None,
+                "traffic": traffic,
+                "peak_source": "measured live: FP32 FMA throughput kernel on this GPU",
+                "flops_per_atom": fl[dom], "ms_per_launch": dom_ms,
+                "hbm": {"achieved": nbytes[dom] * N / (dom_ms * 1e-3) / 1e9,
+                        "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                        "frac": nbytes[dom] * N / (dom_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs"),
+                        "bytes_per_atom": nbytes[dom]}}
+    else:
+        ach = nbytes[dom] * N / (dom_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": kernels[dom], "achieved": ach,
+                "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": ach / peaks.get("hbm_gbs"), "traffic": traffic,
+                "bytes_per_atom": nbytes[dom], "ms_per_launch": dom_ms}
+    plan32.close()
+
+    # ---- plain FP64 path on the same batch
+    plan64, out64, g64 = prepare(FP64)
+    ms64, _ = timed(plan64, out64, max(1, args.fp64_steps), g64)
+    ms64 /= max(1, args.fp64_steps)
+    value64 = world * N / (ms64 * 1e-3)
+    natoms_t = torch.tensor(nat, device=dev, dtype=torch.float64)
+    dE = ((res32["E"] - out64["E"]).abs() / natoms_t)
+    dF = res32["F"] - out64["F"]
+    errors = {"energy_max_eV_per_atom": dE.max().item(),
+              "energy_mean_eV_per_atom": dE.mean().item(),
+              "force_rms_eV_per_A": dF.pow(2).mean().sqrt().item(),
+              "force_max_eV_per_A": dF.abs().max().item(),
+              "force_scale_rms_eV_per_A": out64["F"].pow(2).mean().sqrt().item()}
+    plan64.close()
+
+    # ---- e2e through the C-ABI with host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        lib = _lib.lib()
+        hp = torch.empty((N, 3), dtype=torch.float64, pin_memory=True)
+        hp.copy_(torch.from_numpy(pos))
+        ht = torch.empty(N, dtype=torch.int32, pin_memory=True)
+        ht.copy_(torch.from_numpy(typ))
+        hF = torch.empty((N, 3), dtype=torch.float64, pin_memory=True)
+        hE = torch.empty(S, dtype=torch.float64, pin_memory=True)
+        nat_c = np.ascontiguousarray(nat, dtype=np.int32)
+        cells_c = np.ascontiguousarray(cells.reshape(S, 9))
+        pbc_c = np.ascontiguousarray(pbc, dtype=np.int32)
+        st = C.c_int(0)
+
+        def call():
+            lib.aenet_gpu_batch_energy_forces(
+                S, nat_c.ctypes.data_as(C.c_void_p), C.c_void_p(hp.data_ptr()),
+                C.c_void_p(ht.data_ptr()), cells_c.ctypes.data_as(C.c_void_p),
+                pbc_c.ctypes.data_as(C.c_void_p), MIXED, C.c_void_p(hE.data_ptr()),
+                C.c_void_p(hF.data_ptr()), None, C.byref(st))
+            if st.value:
+                raise RuntimeError("aenet_gpu_batch_energy_forces status %d" % st.value)
+
+        for _ in range(max(1, args.warmup)):
+            call()
+        calls = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call()
+            calls.append(time.perf_counter() - t0)
+        e2e_s = float(np.mean(calls))
+        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * N / tt.item(), "unit": "atoms/s",
+               "h2d_bytes_per_step": N * 24 + N * 4, "d2h_bytes_per_step": S * 8 + N * 24,
+               "ms_per_step": 1e3 * tt.item(), "api": "aenet_gpu_batch_energy_forces"}
+        # same kernels, neighbour order within a cell may differ: FP32 noise
+        dev_e = np.abs(hE.numpy() - res32["E"].cpu().numpy()) / nat
+        assert dev_e.max() < 1e-5, dev_e.max()
+
+    # ---- CPU baseline (rank 0): the oracle port on a bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import Oracle
+        o = Oracle()
+        o.load(w.types, paths)
+        o.set_candidates("cells")
+        threads = os.cpu_count() or 1
+        sample = pick_sample(o, w.structures, threads, args.cpu_seconds)
+        n, dt = time_oracle(o, sample, threads)
+        cpu = {"value": n / dt, "unit": "atoms/s", "cores": threads, "kind": "port",
+               "sample": "first %d of %d cells (%d atoms), FP64 oracle port of predict.x "
+                         "(linked-cell search as written), %d OpenMP threads, %.1f s"
+                         % (len(sample), S, n, threads, dt)}
+        o.close()
+
+    launches_per_step = 7
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic (seeded structures, random-weight networks)",
+                "config": {"workload": WORKLOAD, "nstruc": S, "natoms": N,
+                           "precision": "mixed: fp32 descriptors/networks/forces, fp64 "
+                                        "normalisation shift and per-structure energy sums",
+                           "l2": "512 MB write between timed steps (outside the events); "
+                                 "per-step working set > 1 GB",
+                           "parallelism": "replicas" if world > 1 else "single GPU",
+                           "cuda_graph": not args.no_graph},
+                "fp64": {"value": value64, "unit": "atoms/s", "ms_per_step": ms64},
+                "mixed_over_fp64": value / value64,
+                "errors_vs_fp64": errors, "neighbours": nb,
+                "stages_ms": stages, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+                "wall_s_timed_region": wall}
+        print(json.dumps(line), flush=True)
+    ann.release()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

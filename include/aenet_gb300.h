@@ -114,6 +114,11 @@ int aenet_gpu_plan_profile(aenet_gpu_plan* plan, const double* d_coords,
                            const int* d_types, double* d_E, double* d_F,
                            float* ms, void* stream);
 
+/* Measured FP32 FMA throughput of the current device in TFLOP/s (a
+ * dependent-chain-free FMA loop over every SM); the denominator of the
+ * FP32 roofline of the descriptor kernels. */
+int aenet_gpu_measure_fp32_peak(double* tflops, void* stream);
+
 /* Device status word of the last run: 0, or AENET_GPU_ST_* bits. */
 #define AENET_GPU_ST_NB_OVERFLOW 1u
 #define AENET_GPU_ST_BAD_COORD 2u

@@ -103,3 +103,22 @@ def test_nn_roundtrip_product_writer_oracle_reader(tmp_path, k1, k3):
             np.testing.assert_array_equal(back["stp"]["sfval_avg"], pots[t]["stp"]["sfval_avg"])
             assert back["stp"]["envtypes"] == list(pots[t]["stp"]["envtypes"])
             assert back["ts"]["E_atom"].tolist() == list(pots[t]["ts"]["E_atom"])
+
+
+def test_cell_search_as_written_is_complete_on_small_cells(oracle):
+    """On the batch workload's cells (some shorter than the cut-off) the
+    linked-cell search of lclist.f90 finds the same neighbour sets as the
+    complete search, so the reference's own lists are the oracle's."""
+    from aenet_gb300 import workloads
+    w = workloads.lisio_batch_4096(nstruc=5)
+    from tests.golden import fixtures
+    k1 = fixtures.load("k1_ti2o4.npz")
+    oracle.load(["Ti", "O"], fixtures.potentials(k1))
+    for s in w.structures:
+        sets = []
+        for mode in ("cells", "complete"):
+            oracle.set_candidates(mode)
+            _, _, nb = oracle.neighbors(s.cell, s.positions, np.minimum(s.types, 2))
+            sets.append([sorted(zip(x[2].tolist(), map(tuple, x[0].tolist()))) for x in nb])
+        oracle.set_candidates("complete")
+        assert sets[0] == sets[1]
