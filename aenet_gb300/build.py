@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaenet_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["k_neighbors.cu", "k_chebyshev.cu", "k_behler.cu", "k_mlp.cu", "capi.cpp"]
+SOURCES = ["k_neighbors.cu", "k_cheb_f32.cu", "k_cheb_f64.cu", "k_behler.cu", "k_mlp.cu",
+           "capi.cpp"]
 
 
 def _nvcc():

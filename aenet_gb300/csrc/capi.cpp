@@ -248,6 +248,7 @@ struct State {
   std::vector<HostPot> pots;
   int angular_legacy = 0;
   int cell_div = 2;
+  int lpa_default = 16;
   // device tables
   bool dev_ready = false;
   PotDevice pd{};
@@ -635,6 +636,8 @@ struct aenet_gpu_plan {
   int* cell_atoms = nullptr;
   int ncells = 0, nslots = 0;
   int cap = 0;
+  int cap_a = 0;      // staged angular neighbours per atom
+  int lpa = 0;        // lanes per atom in the descriptor kernels (0 = default)
   int* nb_cnt = nullptr;
   int* nb_jt = nullptr;
   void* nb_vec = nullptr;
@@ -809,6 +812,17 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
     int cap = (int)std::ceil(1.5 * dens_max + 32.0);
     P->cap = (cap + 31) & ~31;
   }
+  if (P->cap_a <= 0) {
+    // angular cut-off of the loaded potentials
+    double arc = 0.0;
+    if (P->pd)
+      for (int t = 0; t < P->pd->ntypes; ++t)
+        arc = std::max(arc, P->pd->sp[t].sftype == AE_SF_CHEBYSHEV ? P->pd->sp[t].cheb.a_Rc : rc);
+    double frac = arc > 0 ? std::pow(std::min(1.0, (arc + 1e-3) / (rc + 1e-3)), 3) : 1.0;
+    int ca = (int)std::ceil(1.5 * dens_max * frac + 16.0);
+    ca = (ca + 7) & ~7;
+    P->cap_a = std::min(ca, P->cap);
+  }
   // layout
   const int N = P->natoms;
   const size_t tsz = P->fp64 ? 8 : 4;
@@ -893,6 +907,7 @@ aenet_gpu_plan* plan_new(int nstruc, const int* natoms, const double* lattices, 
   P->rc = rc;
   P->cell_div = g.cell_div;
   P->cap = cap;
+  P->cap_a = cap > 0 ? cap : 0;   // an explicit capacity (a retry) stages every neighbour
   P->keep_images = keep_images;
   int st = plan_alloc(P.get(), coords0, lattices);
   if (st) {
@@ -911,6 +926,8 @@ DescBuffers desc_buffers(aenet_gpu_plan* P, const double* grad_scale, bool viria
   d.nb_jt = P->nb_jt;
   d.nb_vec = P->nb_vec;
   d.cap = P->cap;
+  d.cap_a = P->cap_a;
+  d.lpa = P->lpa ? P->lpa : g.lpa_default;
   d.G = P->G;
   d.dEdG = P->dEdG;
   d.E_atom = P->E_atom;
@@ -1172,6 +1189,8 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   d.nb_jt = (const int*)(b + o_jt);
   d.nb_vec = b + o_vec;
   d.cap = cap;
+  d.cap_a = cap;
+  d.lpa = 32;
   d.G = b + o_G;
   d.dEdG = b + o_dG;
   d.E_atom = (double*)(b + o_E);
@@ -1399,6 +1418,8 @@ EXPORT void aenet_sfb_eval(int itype0, double coo0[3], int nat, int itype1[], do
   d.nb_jt = (const int*)p_jt;
   d.nb_vec = p_vec;
   d.cap = cap;
+  d.cap_a = cap;
+  d.lpa = 32;
   d.G = p_G;
   int e = ae_launch_chebyshev_forward(pd, d, 1, 0);
   std::vector<double> out(nsf_pad);
@@ -1585,6 +1606,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     else if (v == "current") g.angular_legacy = 0;
     else return AENET_ERR_INPUT;
     g.dev_ready = false;
+    return AENET_OK;
+  }
+  if (k == "lanes_per_atom") {
+    int d = atoi(v.c_str());
+    if (d != 8 && d != 16 && d != 32) return AENET_ERR_INPUT;
+    g.lpa_default = d;
     return AENET_OK;
   }
   if (k == "cell_div") {
@@ -1822,7 +1849,7 @@ int batch_host(int nstruc, const int* natoms, const double* coords, const int* t
     if (status & (AE_ST_BAD_COORD)) return AENET_ERR_INPUT;
     if (status & AE_ST_BAD_TYPE) return AENET_ERR_TYPE;
     if (status & (AE_ST_NB_OVERFLOW | AE_ST_CELL_OVERFLOW)) {
-      // retry with larger capacities
+      // retry with larger capacities (the angular capacity follows cap)
       cap = P->cap * 2;
       c.reset();
       continue;

@@ -157,6 +157,8 @@ struct DescBuffers {
   const int* nb_jt;
   const void* nb_vec;
   int cap;
+  int cap_a;                   // staged angular neighbours per atom
+  int lpa;                     // lanes per atom of the descriptor kernels
   void* G;                     // [N][nsf_pad] (T)
   void* dEdG;                  // [N][nsf_pad] (T)
   double* E_atom;              // [N]

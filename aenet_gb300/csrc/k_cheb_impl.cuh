@@ -1,0 +1,647 @@
+// Chebyshev descriptor (replaces sfb_eval / sfb_radial / sfb_angular of
+// src/ext/sfbasis.f90:440-571, 762-858 and chebyshev.f90:41-128) and its
+// adjoint (the force chain rule of src/aenet.f90:471-477, without ever
+// materialising the descriptor Jacobian).
+//
+// One group of LPA lanes (8, 16 or 32) per central atom.  Radial terms:
+// lanes over neighbours, each lane runs the T_n recurrence for its
+// neighbour and accumulates all orders in registers; a group reduction
+// follows.  In the same pass the neighbours inside the angular cut-off are
+// compacted into shared memory (unit vector, distance, cut-off value and
+// slope, spin, table slot).  Angular terms: the pairs j < k of those are
+// spread over the group's lanes in row-major order of the upper triangle.
+//
+// Feature layout per atom (sfbasis.f90:114-131):
+//   [radial R][angular A][radial x spin R][angular x spin A]
+// The spin block exists when the setup has more than one species;
+// typespin follows sfbasis.f90:142-147.  R and A are compile-time in the
+// exact instantiations (no predicated padding); GUARD instantiations take
+// them at run time up to their template bounds.
+//
+// The adjoint contracts dE/dG (already multiplied by E_scale and the
+// normalisation scale) with the analytic derivatives:
+//   radial:  dE/dd_ij = sum_n g_n (fc' T_n + fc T_n')       along R_ij/d_ij
+//   angular: E_jk = w A(cos), w = fc_j fc_k, A = sum_n g_n T_n
+//            grad_j E_jk = fc_j' fc_k A Rhat_j + w A' (Rhat_k - cos Rhat_j)/d_j
+// Forces of angular neighbours are gathered per staged neighbour in shared
+// memory (the row-side term of a lane's pairs stays in registers until the
+// lane leaves the row) and scattered once; other neighbours receive their
+// radial force directly; the central atom receives minus the sum.
+#pragma once
+#include "common.h"
+
+namespace cheb {
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  using type = float4;
+};
+template <>
+struct Vec4<double> {
+  using type = double4_32a;
+};
+
+// PI as written in sfbasis.f90:72
+constexpr double SFB_PI = 3.14159265358979;
+constexpr double SFB_EPS = 1.0e-12;
+
+__device__ __forceinline__ void sincos_t(float x, float* s, float* c) { __sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_t(double x, double* s, double* c) { sincos(x, s, c); }
+
+template <typename T, int LPA>
+__device__ __forceinline__ T gsum(T v) {
+#pragma unroll
+  for (int d = LPA / 2; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  return v;
+}
+
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, d));
+  return v;
+}
+
+// fc(d) = 0.5 (cos(pi d / Rc) + 1), fc' = -0.5 (pi/Rc) sin(pi d / Rc), zero
+// beyond Rc (sfb_fc / sfb_fc_d1, sfbasis.f90:719-752)
+template <typename T>
+__device__ __forceinline__ void cutoff(T d, T Rc, T& fc, T& dfc) {
+  if (d >= Rc) {
+    fc = T(0);
+    dfc = T(0);
+    return;
+  }
+  const T a = T(SFB_PI) / Rc;
+  T s, c;
+  sincos_t(a * d, &s, &c);
+  fc = T(0.5) * (c + T(1));
+  dfc = T(-0.5) * a * s;
+}
+
+// radial argument x = (2 d - Rc)/Rc of chebyshev_polynomial(d, 0, Rc)
+__device__ __forceinline__ double radial_x(double d, double Rc, double) { return (2.0 * d - Rc) / Rc; }
+__device__ __forceinline__ float radial_x(float d, float, float two_over_rc) {
+  return fmaf(d, two_over_rc, -1.0f);
+}
+
+// angular argument and dx/dcos: current domain [-1, 1] or legacy [0, pi]
+template <typename T>
+__device__ __forceinline__ void angular_arg(T cosv, int legacy, T& x, T& dxdc) {
+  if (legacy) {
+    x = (T(2) * cosv - T(SFB_PI)) / T(SFB_PI);
+    dxdc = T(2) / T(SFB_PI);
+  } else {
+    x = cosv;
+    dxdc = T(1);
+  }
+}
+
+// (G - shift) * scale (sfsetup.f90:985-1035).  FP32 kernels hold the shift
+// as hi + lo floats (FP64 precision); G - hi is exact whenever G and the
+// shift are within a factor two of each other (Sterbenz).
+__device__ __forceinline__ double normalise(double g, const PotDevice& pd, size_t k) {
+  return (g - pd.shift[k]) * pd.scale[k];
+}
+__device__ __forceinline__ float normalise(float g, const PotDevice& pd, size_t k) {
+  const float2 sh = pd.shift2[k];
+  return ((g - sh.x) - sh.y) * pd.scale32[k];
+}
+
+template <typename T>
+struct GroupSmem {
+  typename Vec4<T>::type* au;   // angular neighbours: unit vector, distance
+  typename Vec4<T>::type* af;   // fc, fc', spin, table slot
+  T* fbuf;                      // [cap_a][3] forces on angular neighbours
+  T* g;                         // [nsf_pad] dE/dG
+};
+
+template <typename T>
+__host__ __device__ inline size_t group_smem_bytes(int cap_a, int nsf_pad, bool adjoint) {
+  using T4 = typename Vec4<T>::type;
+  size_t per = 2 * sizeof(T4) * cap_a + (adjoint ? (3 * sizeof(T) * cap_a + sizeof(T) * nsf_pad) : 0);
+  return (per + 31) & ~size_t(31);
+}
+
+template <typename T>
+__device__ __forceinline__ GroupSmem<T> group_smem(unsigned char* base, int cap_a, int nsf_pad,
+                                                   int group, bool adjoint) {
+  using T4 = typename Vec4<T>::type;
+  unsigned char* p = base + group_smem_bytes<T>(cap_a, nsf_pad, adjoint) * group;
+  GroupSmem<T> w;
+  w.au = reinterpret_cast<T4*>(p);
+  w.af = w.au + cap_a;
+  w.fbuf = reinterpret_cast<T*>(w.af + cap_a);
+  w.g = w.fbuf + 3 * cap_a;
+  return w;
+}
+
+// row-major walk of the upper triangle a < b < na with a fixed stride
+struct PairWalk {
+  int a, b;
+  __device__ __forceinline__ void start(int p, int na) {
+    a = 0;
+    int rem = p;
+    while (a < na - 1 && rem >= na - 1 - a) {
+      rem -= na - 1 - a;
+      ++a;
+    }
+    b = a + 1 + rem;
+  }
+  __device__ __forceinline__ void advance(int na, int stride) {
+    b += stride;
+    while (a < na - 1 && b >= na) {
+      b = b - na + a + 2;
+      ++a;
+    }
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void atomic_add3(T* F, int atom, T fx, T fy, T fz);
+template <>
+__device__ __forceinline__ void atomic_add3<float>(float* F, int atom, float fx, float fy, float fz) {
+  atomicAdd(reinterpret_cast<float4*>(F) + atom, make_float4(fx, fy, fz, 0.f));
+}
+template <>
+__device__ __forceinline__ void atomic_add3<double>(double* F, int atom, double fx, double fy,
+                                                    double fz) {
+  atomicAdd(F + 4 * atom, fx);
+  atomicAdd(F + 4 * atom + 1, fy);
+  atomicAdd(F + 4 * atom + 2, fz);
+}
+
+// Radial pass shared by forward and adjoint: lanes over neighbours,
+// compaction of angular neighbours.  `radial` is called for neighbours
+// inside the radial cut-off with (v, s, fc, dfc, x); it returns the force
+// contribution grad_j E to be kept for the neighbour (adjoint) or nothing.
+template <typename T, int LPA>
+struct GroupCtx {
+  int lane, grp, sl, i;
+  bool active;
+};
+
+// ----------------------------------------------------------------------
+// forward
+// ----------------------------------------------------------------------
+template <typename T, int R, int A, int LPA, bool GUARD>
+__global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
+  using T4 = typename Vec4<T>::type;
+  constexpr int GPW = 32 / LPA;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int grp = lane / LPA, sl = lane % LPA;
+  const int wglobal = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (wglobal * GPW >= b.natoms) return;   // whole warp idle
+  const int gid = wglobal * GPW + grp;
+  const bool active = gid < b.natoms;
+  const int i = active ? gid : b.natoms - 1;
+  GroupSmem<T> sm = group_smem<T>(smem_raw, b.cap_a, pd.nsf_pad, warp * GPW + grp, false);
+  const int ti = b.types[i];
+  const ChebTable& ct = pd.sp[ti].cheb;
+  const int n = active ? b.nb_cnt[i] : 0;
+  const int nloop = warp_max(n);
+  const T4* __restrict__ vec = reinterpret_cast<const T4*>(b.nb_vec) + (size_t)i * b.cap;
+  const int* __restrict__ jt = b.nb_jt + (size_t)i * b.cap;
+  const T r_Rc = T(ct.r_Rc), a_Rc = T(ct.a_Rc);
+  const T two_over_rc = T(2) / r_Rc;
+  const int rN = GUARD ? ct.r_N : R;
+  const int aN = GUARD ? ct.a_N : A;
+  const bool multi = ct.multi;
+  const unsigned gmask = (LPA == 32) ? 0xffffffffu : (((1u << LPA) - 1u) << (grp * LPA));
+
+  // ---- radial terms and angular staging
+  T acc[R], accs[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    acc[q] = T(0);
+    accs[q] = T(0);
+  }
+  int na = 0;
+  for (int base = 0; base < nloop; base += LPA) {
+    const int j = base + sl;
+    const bool valid = j < n;
+    T4 v;
+    int t = 0;
+    if (valid) {
+      v = vec[j];
+      t = jt[j] >> AE_TYPE_SHIFT;
+    } else {
+      v.x = v.y = v.z = T(0);
+      v.w = T(1e30);
+    }
+    const T d = v.w;
+    const T s = multi ? T(ct.spin[t]) : T(0);
+    if (d <= r_Rc && d > T(SFB_EPS)) {
+      T fc, dfc;
+      cutoff(d, r_Rc, fc, dfc);
+      const T x = radial_x(d, r_Rc, two_over_rc);
+      const T x2 = x + x;
+      const T sfc = s * fc;
+      T tm1 = T(1), t0 = x;
+      acc[0] += fc;
+      accs[0] += sfc;
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        if (!GUARD || q < rN) {
+          acc[q] = fma(fc, t0, acc[q]);
+          accs[q] = fma(sfc, t0, accs[q]);
+          const T tn = fma(x2, t0, -tm1);
+          tm1 = t0;
+          t0 = tn;
+        }
+      }
+    }
+    const bool inA = d <= a_Rc && d >= T(SFB_EPS);
+    const unsigned m = __ballot_sync(0xffffffffu, inA) & gmask;
+    if (inA) {
+      const int k = na + __popc(m & ((1u << lane) - 1u));
+      if (k < b.cap_a) {
+        const T inv = T(1) / d;
+        T fc, dfc;
+        cutoff(d, a_Rc, fc, dfc);
+        T4 u, f;
+        u.x = v.x * inv;
+        u.y = v.y * inv;
+        u.z = v.z * inv;
+        u.w = d;
+        f.x = fc;
+        f.y = dfc;
+        f.z = s;
+        f.w = T(j);
+        sm.au[k] = u;
+        sm.af[k] = f;
+      }
+    }
+    na += __popc(m);
+  }
+  if (na > b.cap_a) {
+    if (sl == 0 && active) atomicOr(b.status, AE_ST_NB_OVERFLOW);
+    na = b.cap_a;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    acc[q] = gsum<T, LPA>(acc[q]);
+    if (multi) accs[q] = gsum<T, LPA>(accs[q]);
+  }
+  const size_t nrow = (size_t)ti * pd.nsf_pad;
+  T* G = reinterpret_cast<T*>(b.G) + (size_t)i * pd.nsf_pad;
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      if (q % LPA == sl && q < rN) {
+        G[ct.r_i1 + q] = normalise(acc[q], pd, nrow + ct.r_i1 + q);
+        if (multi) G[ct.r_i2 + q] = normalise(accs[q], pd, nrow + ct.r_i2 + q);
+      }
+    }
+  }
+
+  // ---- angular terms
+  T ang[A], angs[A];
+#pragma unroll
+  for (int q = 0; q < A; ++q) {
+    ang[q] = T(0);
+    angs[q] = T(0);
+  }
+  const int P = na * (na - 1) / 2;
+  const int Ploop = warp_max(P);
+  PairWalk pw;
+  pw.start(sl, na);
+  for (int p = sl; p < Ploop; p += LPA) {
+    if (p < P) {
+      const T4 uj = sm.au[pw.a], uk = sm.au[pw.b];
+      const T4 fj = sm.af[pw.a], fk = sm.af[pw.b];
+      const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
+      const T w = fj.x * fk.x;
+      const T sw = fj.z * fk.z * w;
+      T x, dxdc;
+      angular_arg(cosv, ct.angular_legacy, x, dxdc);
+      const T x2 = x + x;
+      T tm1 = T(1), t0 = x;
+      ang[0] += w;
+      angs[0] += sw;
+#pragma unroll
+      for (int q = 1; q < A; ++q) {
+        if (!GUARD || q < aN) {
+          ang[q] = fma(w, t0, ang[q]);
+          angs[q] = fma(sw, t0, angs[q]);
+          const T tn = fma(x2, t0, -tm1);
+          tm1 = t0;
+          t0 = tn;
+        }
+      }
+      pw.advance(na, LPA);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < A; ++q) {
+    ang[q] = gsum<T, LPA>(ang[q]);
+    if (multi) angs[q] = gsum<T, LPA>(angs[q]);
+  }
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < A; ++q) {
+      if (q % LPA == sl && q < aN) {
+        G[ct.a_i1 + q] = normalise(ang[q], pd, nrow + ct.a_i1 + q);
+        if (multi) G[ct.a_i2 + q] = normalise(angs[q], pd, nrow + ct.a_i2 + q);
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------
+// adjoint
+// ----------------------------------------------------------------------
+template <typename T, int R, int A, int LPA, bool GUARD>
+__global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
+  using T4 = typename Vec4<T>::type;
+  constexpr int GPW = 32 / LPA;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int grp = lane / LPA, sl = lane % LPA;
+  const int wglobal = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (wglobal * GPW >= b.natoms) return;
+  const int gid = wglobal * GPW + grp;
+  const bool active = gid < b.natoms;
+  const int i = active ? gid : b.natoms - 1;
+  GroupSmem<T> sm = group_smem<T>(smem_raw, b.cap_a, pd.nsf_pad, warp * GPW + grp, true);
+  const int ti = b.types[i];
+  const ChebTable& ct = pd.sp[ti].cheb;
+  const int n = active ? b.nb_cnt[i] : 0;
+  const int nloop = warp_max(n);
+  const T4* __restrict__ vec = reinterpret_cast<const T4*>(b.nb_vec) + (size_t)i * b.cap;
+  const int* __restrict__ jt = b.nb_jt + (size_t)i * b.cap;
+  const T r_Rc = T(ct.r_Rc), a_Rc = T(ct.a_Rc);
+  const T two_over_rc = T(2) / r_Rc;
+  const int rN = GUARD ? ct.r_N : R;
+  const int aN = GUARD ? ct.a_N : A;
+  const bool multi = ct.multi;
+  const unsigned gmask = (LPA == 32) ? 0xffffffffu : (((1u << LPA) - 1u) << (grp * LPA));
+  const int sid = b.atom_struct[i];
+  const T gs = b.grad_scale ? T(b.grad_scale[sid]) : T(1);
+  const bool want_virial = b.virial != nullptr;
+  T* F = reinterpret_cast<T*>(b.F);
+
+  const T* gsrc = reinterpret_cast<const T*>(b.dEdG) + (size_t)i * pd.nsf_pad;
+  for (int k = sl; k < ct.nsf; k += LPA) sm.g[k] = gs * gsrc[k];
+  __syncwarp();
+  // radial coefficients in registers
+  T gr[R], grs[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    gr[q] = (!GUARD || q < rN) ? sm.g[ct.r_i1 + q] : T(0);
+    grs[q] = (multi && (!GUARD || q < rN)) ? sm.g[ct.r_i2 + q] : T(0);
+  }
+
+  T fix = T(0), fiy = T(0), fiz = T(0);
+  T w00 = 0, w01 = 0, w02 = 0, w10 = 0, w11 = 0, w12 = 0, w20 = 0, w21 = 0, w22 = 0;
+  int na = 0;
+  for (int base = 0; base < nloop; base += LPA) {
+    const int j = base + sl;
+    const bool valid = j < n;
+    T4 v;
+    int t = 0, jatom = 0;
+    if (valid) {
+      v = vec[j];
+      const int q = jt[j];
+      t = q >> AE_TYPE_SHIFT;
+      jatom = q & AE_INDEX_MASK;
+    } else {
+      v.x = v.y = v.z = T(0);
+      v.w = T(1e30);
+    }
+    const T d = v.w;
+    const T s = multi ? T(ct.spin[t]) : T(0);
+    T c = T(0);
+    if (d <= r_Rc && d > T(SFB_EPS)) {
+      T fc, dfc;
+      cutoff(d, r_Rc, fc, dfc);
+      const T x = radial_x(d, r_Rc, two_over_rc);
+      const T x2 = x + x;
+      // T_q and T_q' = q U_{q-1} (chebyshev_polynomial_d1), times dx/dd
+      T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
+      c = (gr[0] + s * grs[0]) * dfc;
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        if (!GUARD || q < rN) {
+          const T gq = gr[q] + s * grs[q];
+          const T dT = T(q) * um1 * two_over_rc;
+          c = fma(gq, fma(dfc, t0, fc * dT), c);
+          const T tn = fma(x2, t0, -tm1);
+          tm1 = t0;
+          t0 = tn;
+          const T un = fma(x2, u0, -um1);
+          um1 = u0;
+          u0 = un;
+        }
+      }
+    }
+    // grad_j E = c R_ij / d; the force on j is minus that
+    const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? c / d : T(0);
+    const T gx = inv * v.x, gy = inv * v.y, gz = inv * v.z;
+    fix += gx;
+    fiy += gy;
+    fiz += gz;
+    const bool inA = d <= a_Rc && d >= T(SFB_EPS);
+    const unsigned m = __ballot_sync(0xffffffffu, inA) & gmask;
+    bool staged = false;
+    if (inA) {
+      const int k = na + __popc(m & ((1u << lane) - 1u));
+      if (k < b.cap_a) {
+        const T invd = T(1) / d;
+        T fc, dfc;
+        cutoff(d, a_Rc, fc, dfc);
+        T4 u, f;
+        u.x = v.x * invd;
+        u.y = v.y * invd;
+        u.z = v.z * invd;
+        u.w = d;
+        f.x = fc;
+        f.y = dfc;
+        f.z = s;
+        f.w = T(j);
+        sm.au[k] = u;
+        sm.af[k] = f;
+        sm.fbuf[3 * k] = -gx;
+        sm.fbuf[3 * k + 1] = -gy;
+        sm.fbuf[3 * k + 2] = -gz;
+        staged = true;
+      }
+    }
+    if (valid && !staged && c != T(0)) {
+      atomic_add3<T>(F, jatom, -gx, -gy, -gz);
+      if (want_virial) {
+        w00 -= v.x * gx; w01 -= v.x * gy; w02 -= v.x * gz;
+        w10 -= v.y * gx; w11 -= v.y * gy; w12 -= v.y * gz;
+        w20 -= v.z * gx; w21 -= v.z * gy; w22 -= v.z * gz;
+      }
+    }
+    na += __popc(m);
+  }
+  if (na > b.cap_a) {
+    if (sl == 0 && active) atomicOr(b.status, AE_ST_NB_OVERFLOW);
+    na = b.cap_a;
+  }
+  __syncwarp();
+
+  // ---- angular pairs
+  const T* ga = sm.g + ct.a_i1;
+  const T* gas = sm.g + ct.a_i2;
+  const int P = na * (na - 1) / 2;
+  const int Ploop = warp_max(P);
+  PairWalk pw;
+  pw.start(sl, na);
+  int cur = -1;
+  T rx = T(0), ry = T(0), rz = T(0);   // force on row neighbour `cur`
+  for (int p = sl; p < Ploop; p += LPA) {
+    if (p < P) {
+      if (pw.a != cur) {
+        if (cur >= 0) {
+          atomicAdd(&sm.fbuf[3 * cur], rx);
+          atomicAdd(&sm.fbuf[3 * cur + 1], ry);
+          atomicAdd(&sm.fbuf[3 * cur + 2], rz);
+        }
+        cur = pw.a;
+        rx = ry = rz = T(0);
+      }
+      const T4 uj = sm.au[pw.a], uk = sm.au[pw.b];
+      const T4 fj = sm.af[pw.a], fk = sm.af[pw.b];
+      const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
+      const T w = fj.x * fk.x;
+      const T ss = fj.z * fk.z;
+      T x, dxdc;
+      angular_arg(cosv, ct.angular_legacy, x, dxdc);
+      const T x2 = x + x;
+      T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
+      T Av = ga[0] + (multi ? ss * gas[0] : T(0));
+      T Bv = T(0);
+#pragma unroll
+      for (int q = 1; q < A; ++q) {
+        if (!GUARD || q < aN) {
+          const T gq = ga[q] + (multi ? ss * gas[q] : T(0));
+          Av = fma(gq, t0, Av);
+          Bv = fma(gq * T(q), um1, Bv);
+          const T tn = fma(x2, t0, -tm1);
+          tm1 = t0;
+          t0 = tn;
+          const T un = fma(x2, u0, -um1);
+          um1 = u0;
+          u0 = un;
+        }
+      }
+      const T dEdc = w * Bv * dxdc;
+      const T dEdj = fj.y * fk.x * Av;
+      const T dEdk = fj.x * fk.y * Av;
+      const T ij = dEdc / uj.w, ik = dEdc / uk.w;
+      const T gjx = dEdj * uj.x + ij * (uk.x - cosv * uj.x);
+      const T gjy = dEdj * uj.y + ij * (uk.y - cosv * uj.y);
+      const T gjz = dEdj * uj.z + ij * (uk.z - cosv * uj.z);
+      const T gkx = dEdk * uk.x + ik * (uj.x - cosv * uk.x);
+      const T gky = dEdk * uk.y + ik * (uj.y - cosv * uk.y);
+      const T gkz = dEdk * uk.z + ik * (uj.z - cosv * uk.z);
+      rx -= gjx;
+      ry -= gjy;
+      rz -= gjz;
+      atomicAdd(&sm.fbuf[3 * pw.b], -gkx);
+      atomicAdd(&sm.fbuf[3 * pw.b + 1], -gky);
+      atomicAdd(&sm.fbuf[3 * pw.b + 2], -gkz);
+      fix += gjx + gkx;
+      fiy += gjy + gky;
+      fiz += gjz + gkz;
+      pw.advance(na, LPA);
+    }
+  }
+  if (cur >= 0) {
+    atomicAdd(&sm.fbuf[3 * cur], rx);
+    atomicAdd(&sm.fbuf[3 * cur + 1], ry);
+    atomicAdd(&sm.fbuf[3 * cur + 2], rz);
+  }
+  __syncwarp();
+
+  // ---- scatter the angular neighbours' forces, virial, central atom
+  if (active) {
+    for (int k = sl; k < na; k += LPA) {
+      const int slot = (int)sm.af[k].w;
+      const T fx = sm.fbuf[3 * k], fy = sm.fbuf[3 * k + 1], fz = sm.fbuf[3 * k + 2];
+      atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
+      if (want_virial) {
+        const T4 v = vec[slot];
+        w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
+        w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
+        w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
+      }
+    }
+  }
+  fix = gsum<T, LPA>(fix);
+  fiy = gsum<T, LPA>(fiy);
+  fiz = gsum<T, LPA>(fiz);
+  if (active && sl == 0) atomic_add3<T>(F, i, fix, fiy, fiz);
+  if (want_virial) {
+    T wv[9] = {w00, w01, w02, w10, w11, w12, w20, w21, w22};
+#pragma unroll
+    for (int q = 0; q < 9; ++q) wv[q] = gsum<T, LPA>(wv[q]);
+    if (active && sl == 0) {
+      double* V = b.virial + 9 * sid;
+#pragma unroll
+      for (int q = 0; q < 9; ++q) atomicAdd(V + q, (double)wv[q]);
+    }
+  }
+}
+
+template <typename T, int R, int A, int LPA, bool GUARD>
+int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
+  const int warps = 4;
+  const int groups = warps * (32 / LPA);
+  size_t smem = group_smem_bytes<T>(b.cap_a, pd.nsf_pad, adjoint) * groups;
+  if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
+  const int atoms_per_block = groups;
+  const int blocks = (b.natoms + atoms_per_block - 1) / atoms_per_block;
+  if (adjoint) {
+    auto kern = k_adjoint<T, R, A, LPA, GUARD>;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<blocks, warps * 32, smem, s>>>(pd, b);
+  } else {
+    auto kern = k_forward<T, R, A, LPA, GUARD>;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<blocks, warps * 32, smem, s>>>(pd, b);
+  }
+  return (int)cudaGetLastError();
+}
+
+template <typename T, int R, int A>
+int launch_lpa(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
+  switch (b.lpa) {
+    case 8: return launch<T, R, A, 8, false>(pd, b, adjoint, s);
+    case 32: return launch<T, R, A, 32, false>(pd, b, adjoint, s);
+    default: return launch<T, R, A, 16, false>(pd, b, adjoint, s);
+  }
+}
+
+// Exact instantiations for the common (radial, angular) sizes, guarded
+// ones for everything else.
+template <typename T>
+int dispatch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
+  int rN = 0, aN = 0;
+  bool same = true;
+  for (int t = 0; t < pd.ntypes; ++t) {
+    if (t > 0 && (pd.sp[t].cheb.r_N != rN || pd.sp[t].cheb.a_N != aN)) same = false;
+    rN = max(rN, pd.sp[t].cheb.r_N);
+    aN = max(aN, pd.sp[t].cheb.a_N);
+  }
+  if (same) {
+    if (rN == 11 && aN == 5) return launch_lpa<T, 11, 5>(pd, b, adjoint, s);
+    if (rN == 13 && aN == 7) return launch_lpa<T, 13, 7>(pd, b, adjoint, s);
+    if (rN == 17 && aN == 9) return launch_lpa<T, 17, 9>(pd, b, adjoint, s);
+    if (rN == 17 && aN == 5) return launch_lpa<T, 17, 5>(pd, b, adjoint, s);
+  }
+  if (rN <= 24 && aN <= 16) return launch<T, 24, 16, 16, true>(pd, b, adjoint, s);
+  if (rN <= 32 && aN <= 32) return launch<T, 32, 32, 16, true>(pd, b, adjoint, s);
+  return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace cheb

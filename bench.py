@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--lanes-per-atom", type=int, default=0,
+                    help="fix the descriptor kernels' lanes per atom (implies --no-tune)")
+    ap.add_argument("--cell-div", type=int, default=0,
+                    help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "aenet_gb300_bench"))
     return ap.parse_args()
 
@@ -105,7 +110,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -264,6 +269,19 @@ def run_gb300(args):
     t = torch.tensor(typ, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
+    tuned = None
+    from aenet_gb300 import core as _core
+    if args.lanes_per_atom or args.cell_div:
+        args.no_tune = True
+        if args.lanes_per_atom:
+            _core.set_option("lanes_per_atom", args.lanes_per_atom)
+        if args.cell_div:
+            _core.set_option("cell_div", args.cell_div)
+        tuned = {"lanes_per_atom": args.lanes_per_atom or None, "cell_div": args.cell_div or None,
+                 "fixed": True}
+    if not args.no_tune:
+        from aenet_gb300 import autotune
+        tuned = autotune.tune(nat, cells, pbc, pos, typ, precision=MIXED, cache=None)
 
     def barrier():
         torch.cuda.synchronize()
@@ -456,7 +474,8 @@ def run_gb300(args):
                            "l2": "512 MB write between timed steps (outside the events); "
                                  "per-step working set > 1 GB",
                            "parallelism": "replicas" if world > 1 else "single GPU",
-                           "cuda_graph": not args.no_graph},
+                           "cuda_graph": not args.no_graph,
+                           "launch_shape": tuned},
                 "fp64": {"value": value64, "unit": "atoms/s", "ms_per_step": ms64},
                 "mixed_over_fp64": value / value64,
                 "errors_vs_fp64": errors, "neighbours": nb,

@@ -221,8 +221,10 @@ def test_aucu4000_mixed_vs_fp64(cuda, oracle, aucu):
 
 
 def test_autograd_adjoint_and_finite_differences(cuda, aucu):
-    """Forces from torch.autograd through the adjoint kernels: equal to the
-    plan's forces, and to central differences (h = 1e-4 A) on 64 atoms."""
+    """Forces from torch.autograd through the adjoint kernels equal the
+    plan's forces, and match central differences (h = 1e-4 A, Richardson
+    extrapolated) of the FP64 energy on 64 random atoms: tightly for the
+    FP64 path, within the mixed-precision force tolerance for FP32."""
     torch = cuda
     from aenet_gb300.core import FP64, MIXED
     from aenet_gb300.plan import Plan, potential_energy
@@ -230,35 +232,35 @@ def test_autograd_adjoint_and_finite_differences(cuda, aucu):
     s = w.structures[0]
     ann = _ann(paths, w.types)
     try:
-        for prec, tol in ((FP64, 1e-6), (MIXED, 3e-2)):
+        types = torch.tensor(s.types, device="cuda", dtype=torch.int32)
+        grads = {}
+        for prec, atol in ((FP64, 1e-9), (MIXED, 1e-3)):
             plan = Plan([s.natoms], [s.cell], precision=prec)
             pos = torch.tensor(s.positions, device="cuda", requires_grad=True)
-            types = torch.tensor(s.types, device="cuda", dtype=torch.int32)
             E = potential_energy(pos, plan, types)
             E.sum().backward()
-            grad = pos.grad.clone()
+            grads[prec] = pos.grad.clone()
             out = plan.run(pos.detach(), types, forces=True)
-            torch.testing.assert_close(grad, -out["F"], rtol=0, atol=1e-12)
-            rng = np.random.default_rng(11)
-            atoms = rng.choice(s.natoms, 64, replace=False)
-            h = 1e-4
-            p0 = pos.detach().clone()
-
-            def central(a, c, hh):
-                pp = p0.clone(); pp[a, c] += hh
-                pm = p0.clone(); pm[a, c] -= hh
-                return (plan.forward(pp, types)[0].item()
-                        - plan.forward(pm, types)[0].item()) / (2 * hh)
-
-            for a in atoms[:16 if prec == MIXED else 64]:
-                c = int(rng.integers(3))
-                if prec == FP64:
-                    # Richardson extrapolation removes the O(h^2) term
-                    fd = (4 * central(a, c, h / 2) - central(a, c, h)) / 3
-                else:
-                    fd = central(a, c, h)
-                assert abs(fd - grad[a, c].item()) < tol, (prec, a, c, fd, grad[a, c].item())
+            # same kernels; in FP32 the atomic summation order differs
+            torch.testing.assert_close(grads[prec], -out["F"], rtol=0, atol=atol)
             plan.close()
+        plan = Plan([s.natoms], [s.cell], precision=FP64)
+        p0 = torch.tensor(s.positions, device="cuda")
+        rng = np.random.default_rng(11)
+        h = 1e-4
+
+        def central(a, c, hh):
+            pp = p0.clone(); pp[a, c] += hh
+            pm = p0.clone(); pm[a, c] -= hh
+            return (plan.forward(pp, types)[0].item()
+                    - plan.forward(pm, types)[0].item()) / (2 * hh)
+
+        for a in rng.choice(s.natoms, 64, replace=False):
+            c = int(rng.integers(3))
+            fd = (4 * central(a, c, h / 2) - central(a, c, h)) / 3
+            assert abs(fd - grads[FP64][a, c].item()) < 1e-6, (a, c, fd)
+            assert abs(fd - grads[MIXED][a, c].item()) < F_RMS_MIXED, (a, c, fd)
+        plan.close()
     finally:
         ann.release()
 
