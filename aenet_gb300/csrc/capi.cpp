@@ -632,9 +632,13 @@ struct aenet_gpu_plan {
   double* r_wrap = nullptr;
   float4* r_f32 = nullptr;
   int* cell_of = nullptr;
+  int* slot_of = nullptr;
   int* cell_count = nullptr;
+  int* cell_start = nullptr;
+  int* scan_tmp = nullptr;
   int* cell_atoms = nullptr;
-  int ncells = 0, nslots = 0;
+  float4* cell_pos = nullptr;
+  int ncells = 0;
   int cap = 0;
   int cap_a = 0;      // staged angular neighbours per atom
   int lpa = 0;        // lanes per atom in the descriptor kernels (0 = default)
@@ -699,8 +703,12 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
   G.rc2 = rcp * rcp;   // (Rc + EPS)*(Rc + EPS), lclist.f90:572
   const double w = rcp / cell_div;
   double ext = rcp;
+  G.rcf = (float)rcp;
   if (pbc) {
     for (int q = 0; q < 9; ++q) G.L[q] = lat[q];
+    G.ortho = (lat[1] == 0.0 && lat[2] == 0.0 && lat[3] == 0.0 && lat[5] == 0.0 &&
+               lat[6] == 0.0 && lat[7] == 0.0 && lat[0] > 0.0 && lat[4] > 0.0 && lat[8] > 0.0)
+                  ? 1 : 0;
     const double* a1 = lat;
     const double* a2 = lat + 3;
     const double* a3 = lat + 6;
@@ -727,6 +735,7 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
     for (int a = 0; a < 3; ++a) {
       double bl = std::sqrt(bb[a][0] * bb[a][0] + bb[a][1] * bb[a][1] + bb[a][2] * bb[a][2]);
       double h = std::fabs(V) / bl;   // height of the cell along axis a
+      G.hf[a] = (float)h;
       int nc = (int)std::floor(h / w);
       if (nc < 1) nc = 1;
       if (nc > 1000) nc = 1000;
@@ -745,9 +754,14 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
         if (i == 0 || x < mn[c]) mn[c] = x;
         if (i == 0 || x > mx[c]) mx[c] = x;
       }
+    // atoms of an isolated structure may leave this box later; their cells
+    // are clamped, which keeps every pair within reach of the full stencil
+    // but not of a pruned one, so no pruning here
+    G.ortho = 0;
     for (int c = 0; c < 3; ++c) {
       G.origin[c] = mn[c] - 0.5 * rcp;
       G.box[c] = (mx[c] - mn[c]) + rcp;
+      G.hf[c] = (float)G.box[c];
       G.L[4 * c] = G.box[c];
       int nc = (int)std::floor(G.box[c] / w);
       if (nc < 1) nc = 1;
@@ -770,7 +784,7 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
 
 int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices) {
   const double rc = P->rc;
-  int cell_off = 0, slot_off = 0, atom_off = 0;
+  int cell_off = 0, atom_off = 0;
   size_t natoms = 0;
   double dens_max = 0;
   for (int s = 0; s < P->nstruc; ++s) {
@@ -780,15 +794,9 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
                        P->natoms_h[s], rc, P->cell_div, 0);
     if (st) return st;
     int nc = G.nc[0] * G.nc[1] * G.nc[2];
-    double expct = (double)P->natoms_h[s] / nc;
-    int cc = (int)std::ceil(3.0 * expct + 16.0);
-    if (cc > P->natoms_h[s]) cc = std::max(1, P->natoms_h[s]);
-    G.cell_cap = cc;
     G.cell_off = cell_off;
-    G.slot_off = slot_off;
     G.atom_off = atom_off;
     cell_off += nc;
-    slot_off += nc * cc;
     atom_off += P->natoms_h[s];
     natoms += P->natoms_h[s];
     double vol;
@@ -807,7 +815,6 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   }
   P->natoms = (int)natoms;
   P->ncells = cell_off;
-  P->nslots = slot_off;
   if (P->cap <= 0) {
     int cap = (int)std::ceil(1.5 * dens_max + 32.0);
     P->cap = (cap + 31) & ~31;
@@ -841,8 +848,12 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_r = take(24 * (size_t)N);
   size_t o_rf = take(16 * (size_t)N);
   size_t o_co = take(4 * (size_t)N);
+  size_t o_so = take(4 * (size_t)N);
   size_t o_cc = take(4 * (size_t)P->ncells);
-  size_t o_ca = take(4 * (size_t)P->nslots);
+  size_t o_cs = take(4 * ((size_t)P->ncells + 1));
+  size_t o_sc = take(4 * ((size_t)P->ncells / 1024 + 2));
+  size_t o_ca = take(4 * (size_t)N);
+  size_t o_cp = take(16 * (size_t)N);
   size_t o_nc = take(4 * (size_t)N);
   size_t o_jt = take(4 * npairs);
   size_t o_vec = take((P->fp64 ? 32 : 16) * npairs);
@@ -864,8 +875,12 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->r_wrap = (double*)(b + o_r);
   P->r_f32 = (float4*)(b + o_rf);
   P->cell_of = (int*)(b + o_co);
+  P->slot_of = (int*)(b + o_so);
   P->cell_count = (int*)(b + o_cc);
+  P->cell_start = (int*)(b + o_cs);
+  P->scan_tmp = (int*)(b + o_sc);
   P->cell_atoms = (int*)(b + o_ca);
+  P->cell_pos = (float4*)(b + o_cp);
   P->nb_cnt = (int*)(b + o_nc);
   P->nb_jt = (int*)(b + o_jt);
   P->nb_vec = (void*)(b + o_vec);
@@ -947,8 +962,12 @@ NbBuffers nb_buffers(aenet_gpu_plan* P) {
   nb.r_wrap = P->r_wrap;
   nb.r_f32 = P->r_f32;
   nb.cell_of = P->cell_of;
+  nb.slot_of = P->slot_of;
   nb.cell_count = P->cell_count;
+  nb.cell_start = P->cell_start;
+  nb.scan_tmp = P->scan_tmp;
   nb.cell_atoms = P->cell_atoms;
+  nb.cell_pos = P->cell_pos;
   nb.ncells_total = P->ncells;
   nb.nstruc = P->nstruc;
   nb.cap = P->cap;
@@ -1498,9 +1517,7 @@ EXPORT void aenet_nbl_init(double latt_vec[9], int natoms, int atom_types[], dou
     // nbl convention afterwards
     StructGeom keep = Pn->geom_h[0];
     if (plan_alloc(Pn.get(), coords, latt_vec)) return;
-    keep.cell_cap = Pn->geom_h[0].cell_cap;
     keep.cell_off = 0;
-    keep.slot_off = 0;
     keep.atom_off = 0;
     Pn->geom_h[0] = keep;
     cudaMemcpy(Pn->geom_d, &keep, sizeof(StructGeom), cudaMemcpyHostToDevice);
@@ -1659,9 +1676,7 @@ EXPORT int aenet_gpu_plan_set_lattices(aenet_gpu_plan* P, const double* lattices
     int st = make_geom(G, lattices + 9 * (size_t)s, 1, nullptr, P->natoms_h[s], P->rc, P->cell_div,
                        O.frac_mode, O.nc);
     if (st) return st;
-    G.cell_cap = O.cell_cap;
     G.cell_off = O.cell_off;
-    G.slot_off = O.slot_off;
     G.atom_off = O.atom_off;
     O = G;
   }

@@ -112,16 +112,17 @@ struct StructGeom {
   double origin[3];   // isolated structures: corner of the binning box
   double box[3];      // isolated structures: edge lengths of the box
   float Lf[9];
+  float hf[3];        // heights of the cell (periodic) or box edges
   double rc2;         // (Rc + 1e-3)^2, the neighbour predicate
   float rc2_lo, rc2_hi;   // FP32 distances in [lo, hi] are decided in FP64
+  float rcf;          // Rc + 1e-3 (pruning of the cell stencil)
   int pbc;
+  int ortho;          // lattice vectors along x, y, z: stencil rows are pruned
   int frac_mode;      // 0: s = (B r)/(2 pi) (predict.x), 1: s = (B r)/(2 pi)
                       // with B without 2 pi (aenet_nbl_init), 2: input is s
   int nc[3];          // cell grid
   int kr[3];          // stencil half width per axis
   int cell_off;       // first cell of this structure in the global grid
-  int cell_cap;       // atom slots per cell
-  int slot_off;       // first slot of this structure's cells
   int atom_off, natoms;
 };
 
@@ -135,8 +136,12 @@ struct NbBuffers {
   double* r_wrap;             // [N][3] Cartesian of the wrapped coordinates
   float4* r_f32;              // [N] (x, y, z, species as int bits)
   int* cell_of;               // [N] packed cell coordinates cx|cy<<10|cz<<20
+  int* slot_of;               // [N] rank of the atom inside its cell
   int* cell_count;            // [ncells_total]
-  int* cell_atoms;            // [nslots]
+  int* cell_start;            // [ncells_total + 1] exclusive prefix of counts
+  int* scan_tmp;              // [scan blocks + 1]
+  int* cell_atoms;            // [N] atoms in cell order
+  float4* cell_pos;           // [N] r_f32 in cell order
   int ncells_total;
   int nstruc;
   int cap;                    // neighbour slots per atom

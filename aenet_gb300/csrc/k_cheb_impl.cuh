@@ -23,10 +23,11 @@
 //   radial:  dE/dd_ij = sum_n g_n (fc' T_n + fc T_n')       along R_ij/d_ij
 //   angular: E_jk = w A(cos), w = fc_j fc_k, A = sum_n g_n T_n
 //            grad_j E_jk = fc_j' fc_k A Rhat_j + w A' (Rhat_k - cos Rhat_j)/d_j
-// Forces of angular neighbours are gathered per staged neighbour in shared
-// memory (the row-side term of a lane's pairs stays in registers until the
-// lane leaves the row) and scattered once; other neighbours receive their
-// radial force directly; the central atom receives minus the sum.
+// In the adjoint the angular term is evaluated two-sided: the lane owning a
+// staged neighbour sweeps all partners and accumulates only that
+// neighbour's gradient, so forces stay in registers (no shared-memory
+// atomics); each neighbour's force is scattered once; the central atom
+// receives minus the sum.
 #pragma once
 #include "common.h"
 
@@ -170,16 +171,6 @@ __device__ __forceinline__ void atomic_add3<double>(double* F, int atom, double 
   atomicAdd(F + 4 * atom + 1, fy);
   atomicAdd(F + 4 * atom + 2, fz);
 }
-
-// Radial pass shared by forward and adjoint: lanes over neighbours,
-// compaction of angular neighbours.  `radial` is called for neighbours
-// inside the radial cut-off with (v, s, fc, dfc, x); it returns the force
-// contribution grad_j E to be kept for the neighbour (adjoint) or nothing.
-template <typename T, int LPA>
-struct GroupCtx {
-  int lane, grp, sl, i;
-  bool active;
-};
 
 // ----------------------------------------------------------------------
 // forward
@@ -487,85 +478,73 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
   }
   __syncwarp();
 
-  // ---- angular pairs
+  // ---- angular terms, two-sided: the lane that owns staged neighbour a
+  // sweeps every partner k != a (all lanes of a group read the same k, a
+  // shared-memory broadcast) and accumulates only grad_a of E_ak, so no
+  // force is ever written by two lanes.
   const T* ga = sm.g + ct.a_i1;
   const T* gas = sm.g + ct.a_i2;
-  const int P = na * (na - 1) / 2;
-  const int Ploop = warp_max(P);
-  PairWalk pw;
-  pw.start(sl, na);
-  int cur = -1;
-  T rx = T(0), ry = T(0), rz = T(0);   // force on row neighbour `cur`
-  for (int p = sl; p < Ploop; p += LPA) {
-    if (p < P) {
-      if (pw.a != cur) {
-        if (cur >= 0) {
-          atomicAdd(&sm.fbuf[3 * cur], rx);
-          atomicAdd(&sm.fbuf[3 * cur + 1], ry);
-          atomicAdd(&sm.fbuf[3 * cur + 2], rz);
-        }
-        cur = pw.a;
-        rx = ry = rz = T(0);
-      }
-      const T4 uj = sm.au[pw.a], uk = sm.au[pw.b];
-      const T4 fj = sm.af[pw.a], fk = sm.af[pw.b];
-      const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
-      const T w = fj.x * fk.x;
-      const T ss = fj.z * fk.z;
-      T x, dxdc;
-      angular_arg(cosv, ct.angular_legacy, x, dxdc);
-      const T x2 = x + x;
-      T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
-      T Av = ga[0] + (multi ? ss * gas[0] : T(0));
-      T Bv = T(0);
+  T gav[A], gasv[A];
 #pragma unroll
-      for (int q = 1; q < A; ++q) {
-        if (!GUARD || q < aN) {
-          const T gq = ga[q] + (multi ? ss * gas[q] : T(0));
-          Av = fma(gq, t0, Av);
-          Bv = fma(gq * T(q), um1, Bv);
-          const T tn = fma(x2, t0, -tm1);
-          tm1 = t0;
-          t0 = tn;
-          const T un = fma(x2, u0, -um1);
-          um1 = u0;
-          u0 = un;
-        }
-      }
-      const T dEdc = w * Bv * dxdc;
-      const T dEdj = fj.y * fk.x * Av;
-      const T dEdk = fj.x * fk.y * Av;
-      const T ij = dEdc / uj.w, ik = dEdc / uk.w;
-      const T gjx = dEdj * uj.x + ij * (uk.x - cosv * uj.x);
-      const T gjy = dEdj * uj.y + ij * (uk.y - cosv * uj.y);
-      const T gjz = dEdj * uj.z + ij * (uk.z - cosv * uj.z);
-      const T gkx = dEdk * uk.x + ik * (uj.x - cosv * uk.x);
-      const T gky = dEdk * uk.y + ik * (uj.y - cosv * uk.y);
-      const T gkz = dEdk * uk.z + ik * (uj.z - cosv * uk.z);
-      rx -= gjx;
-      ry -= gjy;
-      rz -= gjz;
-      atomicAdd(&sm.fbuf[3 * pw.b], -gkx);
-      atomicAdd(&sm.fbuf[3 * pw.b + 1], -gky);
-      atomicAdd(&sm.fbuf[3 * pw.b + 2], -gkz);
-      fix += gjx + gkx;
-      fiy += gjy + gky;
-      fiz += gjz + gkz;
-      pw.advance(na, LPA);
+  for (int q = 0; q < A; ++q) {
+    gav[q] = (!GUARD || q < aN) ? ga[q] : T(0);
+    gasv[q] = (multi && (!GUARD || q < aN)) ? gas[q] : T(0);
+  }
+  const int naloop = warp_max(na);
+  for (int a0 = 0; a0 < naloop; a0 += LPA) {
+    const int a = a0 + sl;
+    const bool own = active && a < na;
+    T4 ua, fa;
+    if (own) {
+      ua = sm.au[a];
+      fa = sm.af[a];
+    } else {
+      ua.x = ua.y = ua.z = T(0);
+      ua.w = T(1);
+      fa.x = fa.y = fa.z = fa.w = T(0);
     }
-  }
-  if (cur >= 0) {
-    atomicAdd(&sm.fbuf[3 * cur], rx);
-    atomicAdd(&sm.fbuf[3 * cur + 1], ry);
-    atomicAdd(&sm.fbuf[3 * cur + 2], rz);
-  }
-  __syncwarp();
-
-  // ---- scatter the angular neighbours' forces, virial, central atom
-  if (active) {
-    for (int k = sl; k < na; k += LPA) {
-      const int slot = (int)sm.af[k].w;
-      const T fx = sm.fbuf[3 * k], fy = sm.fbuf[3 * k + 1], fz = sm.fbuf[3 * k + 2];
+    const T inva = T(1) / ua.w;
+    T gx = T(0), gy = T(0), gz = T(0);
+    for (int k = 0; k < naloop; ++k) {
+      if (own && k < na && k != a) {
+        const T4 uk = sm.au[k];
+        const T4 fk = sm.af[k];
+        const T cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
+        const T w = fa.x * fk.x;
+        const T ss = fa.z * fk.z;
+        T x, dxdc;
+        angular_arg(cosv, ct.angular_legacy, x, dxdc);
+        const T x2 = x + x;
+        T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
+        T Av = gav[0], As = gasv[0], Bv = T(0), Bs = T(0);
+#pragma unroll
+        for (int q = 1; q < A; ++q) {
+          if (!GUARD || q < aN) {
+            Av = fma(gav[q], t0, Av);
+            As = fma(gasv[q], t0, As);
+            const T dq = T(q) * um1;
+            Bv = fma(gav[q], dq, Bv);
+            Bs = fma(gasv[q], dq, Bs);
+            const T tn = fma(x2, t0, -tm1);
+            tm1 = t0;
+            t0 = tn;
+            const T un = fma(x2, u0, -um1);
+            um1 = u0;
+            u0 = un;
+          }
+        }
+        Av = fma(ss, As, Av);
+        Bv = fma(ss, Bs, Bv);
+        const T dEda = fa.y * fk.x * Av;         // d/dd_a of w A
+        const T dEdc = w * Bv * dxdc * inva;     // (dE/dcos) / d_a
+        gx += dEda * ua.x + dEdc * (uk.x - cosv * ua.x);
+        gy += dEda * ua.y + dEdc * (uk.y - cosv * ua.y);
+        gz += dEda * ua.z + dEdc * (uk.z - cosv * ua.z);
+      }
+    }
+    if (own) {
+      const int slot = (int)fa.w;
+      const T fx = sm.fbuf[3 * a] - gx, fy = sm.fbuf[3 * a + 1] - gy, fz = sm.fbuf[3 * a + 2] - gz;
       atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
       if (want_virial) {
         const T4 v = vec[slot];
@@ -573,6 +552,9 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
         w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
         w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
       }
+      fix += gx;
+      fiy += gy;
+      fiz += gz;
     }
   }
   fix = gsum<T, LPA>(fix);

@@ -11,14 +11,20 @@
 // cut-off to the FP64 test.
 //
 // Kernels:
-//   k_wrap_bin    one thread per atom: lattice coordinates
-//                 (geometry.f90:697-712), wrap, Cartesian of the wrapped
-//                 coordinates, append to a fixed-capacity cell slot list
-//   k_neighbors   one warp per atom: enumerate the stencil of cells around
-//                 the atom's cell (each offset is a distinct (cell, image)
-//                 pair), flatten their atoms into one candidate index space
-//                 processed 32 at a time, filter, compact with ballots into
-//                 the atom's ELL row.
+//   k_wrap_bin     one thread per atom: lattice coordinates
+//                  (geometry.f90:697-712), wrap, Cartesian of the wrapped
+//                  coordinates, cell, rank inside the cell (atomic count)
+//   k_scan_*       exclusive prefix sum of the cell counts (CSR offsets)
+//   k_scatter      atoms and their FP32 positions in cell order
+//   k_neighbors    one warp per atom.  The stencil of cells around the
+//                  atom's cell is walked as units (row d0, d1; image t2 along
+//                  the third axis): each unit is one contiguous run of cells
+//                  and therefore one contiguous range of atoms.  For
+//                  orthogonal cells each row is cut to the part of the
+//                  cut-off sphere it can reach from the atom.  The ranges of
+//                  32 units are flattened into one candidate index space
+//                  processed 32 candidates at a time; accepted neighbours are
+//                  compacted with ballots into the atom's ELL row.
 #include "common.h"
 
 namespace {
@@ -28,17 +34,14 @@ constexpr double TWO_PI = 6.283185307179586;  // 2 * 3.141592653589793
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 
-// s = (B r) / (2 pi) then wrapped into [0, 1): the matmul of
-// geometry.f90:708 summed in column order, the loops of lclist.f90:953-987
-// (s - floor(s) gives the same value as repeated +-1.0, see the note in
-// wrap_coordinate).
+// wrap into [0, 1) as the loops of lclist.f90:953-987 do: for |s| >= 1
+// every step of the repeated +-1.0 is exact and for s in [-1, 0) both forms
+// round s + 1 once, so s - floor(s) gives the same value.
 __device__ __forceinline__ double wrap_coordinate(double s, unsigned* status) {
   if (!isfinite(s)) {
     atomicOr(status, AE_ST_BAD_COORD);
     return 0.0;
   }
-  // For |s| >= 1 every step of the reference's repeated +-1.0 is exact, and
-  // for s in [-1, 0) both forms round s + 1 once; so they agree bitwise.
   double f = floor(s);
   double w = da(s, -f);
   if (w >= 1.0) w = da(w, -1.0);
@@ -53,13 +56,14 @@ __global__ void k_wrap_bin(int natoms, const double* __restrict__ pos,
   const StructGeom* g = nb.geom + nb.atom_struct[i];
   double r[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
   double s[3], rw[3];
-  int nc[3] = {g->nc[0], g->nc[1], g->nc[2]};
+  const int nc[3] = {g->nc[0], g->nc[1], g->nc[2]};
   if (g->pbc) {
     for (int v = 0; v < 3; ++v) {
       double t;
       if (g->frac_mode == 2) {
         t = r[v];
       } else {
+        // (B r) summed in column order (geometry.f90:708)
         t = dm(g->B[3 * v], r[0]);
         t = da(t, dm(g->B[3 * v + 1], r[1]));
         t = da(t, dm(g->B[3 * v + 2], r[2]));
@@ -86,22 +90,92 @@ __global__ void k_wrap_bin(int natoms, const double* __restrict__ pos,
   int cc[3];
   for (int v = 0; v < 3; ++v) {
     double x = floor(s[v] * (double)nc[v]);
-    int c = x < 0.0 ? 0 : (x >= (double)(nc[v] - 1) ? nc[v] - 1 : (int)x);
-    cc[v] = c;
+    cc[v] = x < 0.0 ? 0 : (x >= (double)(nc[v] - 1) ? nc[v] - 1 : (int)x);
   }
-  int lin = (cc[0] * nc[1] + cc[1]) * nc[2] + cc[2];
-  int slot = atomicAdd(&nb.cell_count[g->cell_off + lin], 1);
-  if (slot < g->cell_cap)
-    nb.cell_atoms[g->slot_off + lin * g->cell_cap + slot] = i;
-  else
-    atomicOr(nb.status, AE_ST_CELL_OVERFLOW);
-  int t = types[i];
+  const int lin = (cc[0] * nc[1] + cc[1]) * nc[2] + cc[2];
+  nb.slot_of[i] = atomicAdd(&nb.cell_count[g->cell_off + lin], 1);
+  const int t = types[i];
   for (int v = 0; v < 3; ++v) {
     nb.s_wrap[3 * i + v] = s[v];
     nb.r_wrap[3 * i + v] = rw[v];
   }
   nb.r_f32[i] = make_float4((float)rw[0], (float)rw[1], (float)rw[2], __int_as_float(t));
   nb.cell_of[i] = cc[0] | (cc[1] << 10) | (cc[2] << 20);
+}
+
+// ---- exclusive scan of the cell counts (three phases, 1024 per block)
+constexpr int SCAN_B = 1024;
+
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int u = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += u;
+  }
+  return v;
+}
+
+// block-wide exclusive scan of one value per thread (blockDim.x == 1024)
+__device__ __forceinline__ int block_excl_scan(int v, int* warp_tot, int& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int incl = warp_incl_scan(v, lane);
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int wv = warp_tot[lane];
+    int wi = warp_incl_scan(wv, lane);
+    warp_tot[lane] = wi - wv;
+    if (lane == 31) warp_tot[32] = wi;
+  }
+  __syncthreads();
+  total = warp_tot[32];
+  int r = warp_tot[warp] + incl - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(SCAN_B) k_scan_blocks(int n, const int* __restrict__ in,
+                                                       int* __restrict__ out,
+                                                       int* __restrict__ bsum) {
+  __shared__ int wt[33];
+  const int e = blockIdx.x * SCAN_B + threadIdx.x;
+  const int v = e < n ? in[e] : 0;
+  int total;
+  const int ex = block_excl_scan(v, wt, total);
+  if (e < n) out[e] = ex;
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_B) k_scan_sums(int nb, int* __restrict__ bsum,
+                                                     int* __restrict__ out_total) {
+  __shared__ int wt[33];
+  int carry = 0;
+  for (int base = 0; base < nb; base += SCAN_B) {
+    const int e = base + threadIdx.x;
+    const int v = e < nb ? bsum[e] : 0;
+    int total;
+    const int ex = block_excl_scan(v, wt, total);
+    if (e < nb) bsum[e] = ex + carry;
+    carry += total;
+  }
+  if (threadIdx.x == 0) *out_total = carry;
+}
+
+__global__ void k_scan_add(int n, int* __restrict__ out, const int* __restrict__ bsum) {
+  const int e = blockIdx.x * SCAN_B + threadIdx.x;
+  if (e < n) out[e] += bsum[blockIdx.x];
+}
+
+__global__ void k_scatter(int natoms, NbBuffers nb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  const StructGeom* g = nb.geom + nb.atom_struct[i];
+  const int packed = nb.cell_of[i];
+  const int c0 = packed & 1023, c1 = (packed >> 10) & 1023, c2 = (packed >> 20) & 1023;
+  const int lin = (c0 * g->nc[1] + c1) * g->nc[2] + c2;
+  const int p = nb.cell_start[g->cell_off + lin] + nb.slot_of[i];
+  nb.cell_atoms[p] = i;
+  nb.cell_pos[p] = nb.r_f32[i];
 }
 
 __device__ __forceinline__ int floor_div(int a, int n) {
@@ -129,67 +203,98 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
   const int pbc = g->pbc;
   const int nc0 = g->nc[0], nc1 = g->nc[1], nc2 = g->nc[2];
   const int k0 = g->kr[0], k1 = g->kr[1], k2 = g->kr[2];
-  const int w0 = 2 * k0 + 1, w1 = 2 * k1 + 1, w2 = 2 * k2 + 1;
-  const int noff = w0 * w1 * w2;
+  const int w1 = 2 * k1 + 1;
   const int packed = nb.cell_of[i];
   const int c0 = packed & 1023, c1 = (packed >> 10) & 1023, c2 = (packed >> 20) & 1023;
+  // images along the third axis reachable from this cell
+  const int t2lo = pbc ? floor_div(c2 - k2, nc2) : 0;
+  const int t2hi = pbc ? floor_div(c2 + k2, nc2) : 0;
+  const int nt2 = t2hi - t2lo + 1;
+  const int nunits = (2 * k0 + 1) * w1 * nt2;
   const float4 ri = nb.r_f32[i];
   const float rc2_lo = g->rc2_lo, rc2_hi = g->rc2_hi;
   const double rc2 = g->rc2;
   const int cap = nb.cap;
   const size_t row = (size_t)i * cap;
+  const int* __restrict__ cstart = nb.cell_start + g->cell_off;
+  // lattice coordinates of the atom (pruning in orthogonal cells; the cut
+  // is widened slightly so that rounding can only keep extra candidates)
+  const float sf0 = (float)nb.s_wrap[3 * i], sf1 = (float)nb.s_wrap[3 * i + 1],
+              sf2 = (float)nb.s_wrap[3 * i + 2];
+  const float rcf = g->rcf * 1.0001f + 1e-4f;
   int cnt = 0;
 
-  for (int obase = 0; obase < noff; obase += 32) {
-    // ---- this lane's stencil offset: target cell, image, atom count
-    int o = obase + lane;
-    int cnt_o = 0, slot0 = 0, T0 = 0, T1 = 0, T2 = 0;
+  for (int ubase = 0; ubase < nunits; ubase += 32) {
+    // ---- this lane's unit: cells [zlo, zhi] of row (d0, d1), image t2
+    const int u = ubase + lane;
+    int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
     float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
-    if (o < noff) {
-      int d2 = o % w2 - k2;
-      int d1 = (o / w2) % w1 - k1;
-      int d0 = o / (w2 * w1) - k0;
-      int a0 = c0 + d0, a1 = c1 + d1, a2 = c2 + d2;
+    if (u < nunits) {
+      const int it2 = u % nt2;
+      const int rr = u / nt2;
+      const int d1 = rr % w1 - k1;
+      const int d0 = rr / w1 - k0;
+      int a0 = c0 + d0, a1 = c1 + d1;
       bool ok = true;
-      if (pbc) {
-        T0 = floor_div(a0, nc0); a0 -= T0 * nc0;
-        T1 = floor_div(a1, nc1); a1 -= T1 * nc1;
-        T2 = floor_div(a2, nc2); a2 -= T2 * nc2;
-      } else {
-        ok = a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1 && a2 >= 0 && a2 < nc2;
+      int zlo = c2 - k2, zhi = c2 + k2;   // unwrapped cell indices
+      if (g->ortho) {
+        const float x0 = (float)a0 / nc0, x1 = (float)(a0 + 1) / nc0;
+        const float y0 = (float)a1 / nc1, y1 = (float)(a1 + 1) / nc1;
+        const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * g->hf[0];
+        const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * g->hf[1];
+        const float rem = rcf * rcf - gx * gx - gy * gy;
+        if (rem < 0.f) {
+          ok = false;
+        } else {
+          const float hz = sqrtf(rem) / g->hf[2] * 1.0001f + 1e-6f;
+          zlo = max(zlo, (int)floorf((sf2 - hz) * nc2));
+          zhi = min(zhi, (int)floorf((sf2 + hz) * nc2));
+        }
       }
-      if (ok) {
-        int lin = (a0 * nc1 + a1) * nc2 + a2;
-        cnt_o = min(nb.cell_count[g->cell_off + lin], g->cell_cap);
-        slot0 = g->slot_off + lin * g->cell_cap;
-        float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
+      if (pbc) {
+        T0 = floor_div(a0, nc0);
+        a0 -= T0 * nc0;
+        T1 = floor_div(a1, nc1);
+        a1 -= T1 * nc1;
+        T2 = t2lo + it2;
+        zlo = max(zlo, T2 * nc2);
+        zhi = min(zhi, T2 * nc2 + nc2 - 1);
+      } else {
+        ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
+        zlo = max(zlo, 0);
+        zhi = min(zhi, nc2 - 1);
+      }
+      if (ok && zlo <= zhi) {
+        const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
+        beg = cstart[base + zlo];
+        len = cstart[base + zhi + 1] - beg;
+        const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
         sh0 = f0 * g->Lf[0] + f1 * g->Lf[3] + f2 * g->Lf[6];
         sh1 = f0 * g->Lf[1] + f1 * g->Lf[4] + f2 * g->Lf[7];
         sh2 = f0 * g->Lf[2] + f1 * g->Lf[5] + f2 * g->Lf[8];
       }
     }
-    // inclusive prefix of counts over the 32 offsets of this chunk
-    int incl = cnt_o;
+    int incl = len;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      int v = __shfl_up_sync(0xffffffffu, incl, d);
-      if (lane >= d) incl += v;
+      const int w = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += w;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     for (int qb = 0; qb < total; qb += 32) {
       const int q = qb + lane;
-      // owner offset: first lane whose inclusive prefix exceeds q
+      // owner unit: first lane whose inclusive prefix exceeds q
       int lo = 0, hi = 31;
 #pragma unroll
       for (int step = 0; step < 5; ++step) {
-        int mid = (lo + hi) >> 1;
-        int pv = __shfl_sync(0xffffffffu, incl, mid);
+        const int mid = (lo + hi) >> 1;
+        const int pv = __shfl_sync(0xffffffffu, incl, mid);
         if (pv > q) hi = mid; else lo = mid + 1;
       }
       const int own = lo;
       const int own_incl = __shfl_sync(0xffffffffu, incl, own);
-      const int own_cnt = __shfl_sync(0xffffffffu, cnt_o, own);
-      const int own_slot = __shfl_sync(0xffffffffu, slot0, own);
+      const int own_len = __shfl_sync(0xffffffffu, len, own);
+      const int own_beg = __shfl_sync(0xffffffffu, beg, own);
       const int oT0 = __shfl_sync(0xffffffffu, T0, own);
       const int oT1 = __shfl_sync(0xffffffffu, T1, own);
       const int oT2 = __shfl_sync(0xffffffffu, T2, own);
@@ -197,14 +302,16 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
       const float osh1 = __shfl_sync(0xffffffffu, sh1, own);
       const float osh2 = __shfl_sync(0xffffffffu, sh2, own);
       bool accept = false;
-      int j = -1;
+      int j = -1, tj = 0;
       float dx = 0.f, dy = 0.f, dz = 0.f, dd2 = 0.f;
       if (q < total) {
-        j = nb.cell_atoms[own_slot + (q - (own_incl - own_cnt))];
+        const int p = own_beg + (q - (own_incl - own_len));
+        const float4 rj = nb.cell_pos[p];
+        j = nb.cell_atoms[p];
+        tj = __float_as_int(rj.w);
         const bool self_img = (j == i);
         const bool zeroT = (oT0 == 0 && oT1 == 0 && oT2 == 0);
         if (!(self_img && zeroT)) {
-          const float4 rj = nb.r_f32[j];
           dx = (rj.x - ri.x) + osh0;
           dy = (rj.y - ri.y) + osh1;
           dz = (rj.z - ri.z) + osh2;
@@ -249,13 +356,12 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
       if (accept) {
         const int k = cnt + __popc(mask & ((1u << lane) - 1u));
         if (k < cap) {
-          const int tj = __float_as_int(nb.r_f32[j].w);
           nb.nb_jt[row + k] = j | (tj << AE_TYPE_SHIFT);
           if (nb.nb_img)
             nb.nb_img[row + k] = (oT0 & 1023) | ((oT1 & 1023) << 10) | ((oT2 & 1023) << 20);
           if (VecOut<T4>::fp64) {
-            // R_ij = L (s_j + T) - L s_i in FP64 (the coordinates the
-            // descriptor of the reference sees)
+            // R_ij = L (s_j + T) - L s_i in FP64 (the vectors the reference's
+            // descriptor sees)
             double R[3];
             if (pbc) {
               const double* sj = nb.s_wrap + 3 * j;
@@ -271,7 +377,8 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
               for (int c = 0; c < 3; ++c) R[c] = da(nb.r_wrap[3 * j + c], -nb.r_wrap[3 * i + c]);
             }
             double dist = sqrt(da(da(dm(R[0], R[0]), dm(R[1], R[1])), dm(R[2], R[2])));
-            reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] = make_double4_32a(R[0], R[1], R[2], dist);
+            reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] =
+                make_double4_32a(R[0], R[1], R[2], dist);
           } else {
             reinterpret_cast<float4*>(nb.nb_vec)[row + k] = make_float4(dx, dy, dz, sqrtf(dd2));
           }
@@ -288,13 +395,20 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
 
 }  // namespace
 
-int ae_launch_neighbors(int natoms, const double* pos, const int* types,
-                        const NbBuffers& nb, int fp64, cudaStream_t s) {
+int ae_launch_neighbors(int natoms, const double* pos, const int* types, const NbBuffers& nb,
+                        int fp64, cudaStream_t s) {
   if (natoms <= 0) return 0;
-  cudaError_t e = cudaMemsetAsync(nb.cell_count, 0, sizeof(int) * (size_t)nb.ncells_total, s);
+  const int nc = nb.ncells_total;
+  cudaError_t e = cudaMemsetAsync(nb.cell_count, 0, sizeof(int) * (size_t)nc, s);
   if (e != cudaSuccess) return (int)e;
   k_wrap_bin<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, pos, types, nb);
-  int blocks = (natoms + 7) / 8;
+  // CSR offsets: cell_start[c] = sum of the counts before c, cell_start[nc] = natoms
+  const int nblk = (nc + SCAN_B - 1) / SCAN_B;
+  k_scan_blocks<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_count, nb.cell_start, nb.scan_tmp);
+  k_scan_sums<<<1, SCAN_B, 0, s>>>(nblk, nb.scan_tmp, nb.cell_start + nc);
+  k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
+  k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
+  const int blocks = (natoms + 7) / 8;
   if (fp64)
     k_neighbors<double4_32a><<<blocks, 256, 0, s>>>(natoms, nb);
   else

@@ -133,6 +133,9 @@ def test_neighbour_sets_bit_exact(cuda, oracle, cu256):
         cases.append((cell, pos, np.ones(n, dtype=np.int32)))
     tric = np.array([[5.1, 0.0, 0.0], [1.7, 4.9, 0.0], [-1.2, 0.8, 6.3]])
     cases.append((tric, rng.uniform(0, 5, (30, 3)), np.ones(30, dtype=np.int32)))
+    # orthorhombic, different heights per axis (pruned stencil rows)
+    box = np.diag([18.3, 25.1, 31.7])
+    cases.append((box, rng.uniform(0, 1, (900, 3)) @ box, np.ones(900, dtype=np.int32)))
     ann = _ann(paths, w.types)
     oracle.load(w.types, paths)
     try:
@@ -342,5 +345,30 @@ def test_capacity_overflow_is_reported_and_retried(cuda, cu256):
         # the host-buffer entry point resizes and retries on its own
         r = ann.structure_energy_forces(s.positions * 0.6, s.types, s.cell * 0.6, precision=FP64)
         assert np.isfinite(r["energy"])
+    finally:
+        ann.release()
+
+
+def test_fp32_and_fp64_plans_find_the_same_neighbours(cuda, oracle, tmp_path):
+    """Both precisions decide the cut-off with the same FP64 predicate."""
+    torch = cuda
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED
+    from aenet_gb300.plan import Plan
+    w = workloads.lisio_batch_4096(nstruc=64)
+    paths = helpers.make_potentials(oracle, w, str(tmp_path), max_atoms=500)
+    ann = _ann(paths, w.types)
+    try:
+        nat, pos, typ, cells, pbc = w.packed()
+        p = torch.tensor(pos, device="cuda")
+        t = torch.tensor(typ, device="cuda")
+        counts = []
+        for prec in (FP64, MIXED):
+            plan = Plan(nat, cells, pbc, precision=prec)
+            plan.run(p, t)
+            plan.check()
+            counts.append(plan.neighbors()[1].clone())
+            plan.close()
+        assert torch.equal(counts[0], counts[1])
     finally:
         ann.release()
