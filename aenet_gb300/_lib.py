@@ -90,6 +90,9 @@ def _declare(lib):
     lib.aenet_gpu_plan_neighbors.restype = C.c_int
     lib.aenet_gpu_plan_descriptors.argtypes = [vp, C.POINTER(vp), ip]
     lib.aenet_gpu_plan_descriptors.restype = C.c_int
+    lib.aenet_gpu_structure_energy_forces_noalloc.argtypes = [C.c_int, vp, vp, vp, C.c_int, vp, vp,
+                                                              vp, vp, vp]
+    lib.aenet_gpu_structure_energy_forces_noalloc.restype = C.c_int
     return lib
 
 
@@ -118,4 +121,5 @@ def exported_symbols():
             names.append(m.group(1))
         for m in re.finditer(r"extern\s+\w+\s+(\w+)\s*;", txt):
             names.append(m.group(1))
-    return sorted(set(n for n in names if not n.startswith("AENET_GPU_") or n.endswith("_H")))
+    return sorted(set(n for n in names
+                       if not (n.startswith("AENET_GPU_") or n.startswith("AENET_NOALLOC_"))))

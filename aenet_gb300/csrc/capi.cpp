@@ -1781,6 +1781,27 @@ EXPORT int aenet_gpu_plan_descriptors(aenet_gpu_plan* P, const void** d_G, int* 
   return 0;
 }
 
+// ---- internal accessors used by noalloc.cu ----------------------------
+
+// Copy of the device tables of the loaded potentials and the neighbour
+// cut-off; returns 0 when the tables exist (they are built by the first
+// evaluation after loading), AENET_ERR_INIT otherwise.  Never allocates.
+int ae_device_tables(PotDevice* out, double* rc, int* cell_div) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!(g.init && g.loaded && g.dev_ready)) return AENET_ERR_INIT;
+  *out = g.pd;
+  *rc = aenet_Rc_max;
+  *cell_div = g.cell_div;
+  return 0;
+}
+
+int ae_lanes_per_atom() { return g.lpa_default; }
+
+// Geometry of one periodic structure (host arithmetic only).
+int ae_periodic_geom(StructGeom* G, const double* lattice, int natoms, double rc, int cell_div) {
+  return make_geom(*G, lattice, 1, nullptr, natoms, rc, cell_div, 0);
+}
+
 // ---- host-buffer entry points ----------------------------------------
 
 namespace {

@@ -138,6 +138,42 @@ int aenet_gpu_plan_neighbors(aenet_gpu_plan* plan, int* cap,
 int aenet_gpu_plan_descriptors(aenet_gpu_plan* plan, const void** d_G,
                                int* nsf_pad);
 
+/* ---- evaluation without device memory allocation ---------------------
+ * No counterpart in the reference (aenet runs on the CPU and allocates its
+ * work arrays per call).  For callers that cannot allocate device memory
+ * while they run -- MD engines that reserve all GPU memory at start-up and
+ * forbid cudaMalloc in the time loop, hosts that capture their step in a
+ * CUDA graph, plugins whose host owns the memory pool -- this computes the
+ * energy and forces of ONE periodic structure using only the caller's
+ * device buffers plus a fixed scratch array compiled into the library
+ * (about 19 MB per GPU, held until the process exits).
+ *
+ * Inputs (device): d_coords[3*natoms] Cartesian, d_types[natoms] 1-based;
+ * lattice[9] (HOST) rows = lattice vectors.  Outputs (device, any may be
+ * NULL): *d_E total energy, d_F[3*natoms], d_virial[9], *d_status (the
+ * AENET_GPU_ST_* word of this run).  Work is queued on `stream`; the call
+ * returns without synchronising.
+ *
+ * Limits: natoms <= AENET_NOALLOC_MAX_ATOMS, at most
+ * AENET_NOALLOC_MAX_NEIGHBORS neighbours per atom (more sets
+ * AENET_GPU_ST_NB_OVERFLOW in *d_status), at most AENET_NOALLOC_MAX_CELLS
+ * neighbour-grid cells; larger inputs return AENET_ERR_MALLOC at once.
+ * The potentials must be loaded and one allocating evaluation must have
+ * run first (it builds the device tables): otherwise AENET_ERR_INIT.
+ * The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one scratch array: calls that overlap on the GPU
+ * (different streams, threads) race and give wrong results. */
+#define AENET_NOALLOC_MAX_ATOMS 2048
+#define AENET_NOALLOC_MAX_NEIGHBORS 192
+#define AENET_NOALLOC_MAX_CELLS 65536
+int aenet_gpu_structure_energy_forces_noalloc(int natoms, const double* d_coords,
+                                              const int* d_types,
+                                              const double* lattice,
+                                              int precision, double* d_E,
+                                              double* d_F, double* d_virial,
+                                              unsigned* d_status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
