@@ -480,6 +480,24 @@ int ensure_device() {
 // Behler tables (defined after the anonymous namespace helpers)
 // ---------------------------------------------------------------------
 namespace {
+BehlerFn make_fn(double Rc, double p1, double p2, double p3, int kind, int out) {
+  BehlerFn b{};
+  b.Rc = Rc;
+  b.p1 = p1;
+  b.p2 = p2;
+  b.p3 = p3;
+  b.fRc = (float)Rc;
+  b.fp1 = (float)p1;
+  b.fp2 = (float)p2;
+  b.fp3 = (float)p3;
+  b.kind = kind;
+  b.out = out;
+  // G4/G5 zeta (p2) evaluated by repeated squaring when it is a small integer
+  b.izeta = 0;
+  if ((kind == 4 || kind == 5) && p2 >= 1.0 && p2 <= 64.0 && p2 == std::floor(p2)) b.izeta = (int)p2;
+  return b;
+}
+
 int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out) {
   // sf_init over the global types (sfsetup.f90:800-808, symmfunc.f90:91-140)
   const int nt = g.ntypes;
@@ -576,9 +594,8 @@ int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<doubl
       int iG = iG02[pij];
       for (int kd = 1; kd <= 3; ++kd)
         for (auto& f : rad[pij][kd]) {
-          BehlerFn b{f.Rc, f.p1, f.p2, f.p3, kd, iG++};
+          fns.push_back(make_fn(f.Rc, f.p1, f.p2, f.p3, kd, iG++));
           rcm = std::max(rcm, f.Rc);
-          fns.push_back(b);
         }
     }
     for (int gj = 0; gj < nt; ++gj)
@@ -590,9 +607,8 @@ int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<doubl
         int iG = iG03[tijk];
         for (int kd = 4; kd <= 5; ++kd)
           for (auto& f : ang[tijk][kd]) {
-            BehlerFn b{f.Rc, f.p1, f.p2, f.p3, kd, iG++};
+            fns.push_back(make_fn(f.Rc, f.p1, f.p2, f.p3, kd, iG++));
             rcm = std::max(rcm, f.Rc);
-            fns.push_back(b);
           }
       }
     hdr.ang_off[nt * nt] = (int)fns.size();

@@ -19,7 +19,7 @@
 #include <stdint.h>
 
 #define AE_MAXT 8            // species per potential set
-#define AE_MAXNSF 128        // descriptor length
+#define AE_MAXNSF 160        // descriptor length
 #define AE_MAXLAYERS 8       // network layers including input and output
 #define AE_MAXNODES 64       // nodes per hidden layer
 #define AE_MAXCHEB 32        // Chebyshev order + 1
@@ -52,8 +52,11 @@ struct ChebTable {
 
 struct BehlerFn {     // one radial (G1..G3) or angular (G4, G5) function
   double Rc, p1, p2, p3;  // G2: Rs, eta; G3: kappa; G4/G5: lambda, zeta, eta
+  float fRc, fp1, fp2, fp3;   // the same parameters rounded to float
   int kind;               // 1..5
   int out;                // feature index (reference order)
+  int izeta;              // zeta as an integer in [1, 64] when it is one, else 0
+  int pad;
 };
 
 // Per central species: functions grouped by neighbour species (radial) and

@@ -172,10 +172,10 @@ def behler_functions(types, rc=6.5):
     return funcs
 
 
-def tio2_rutile_9000(seed=3):
+def tio2_rutile_9000(seed=3, cells=(10, 10, 15)):
     rng = np.random.default_rng(seed)
     types = ["Ti", "O"]
-    pos, species, cell = rutile_positions(10, 10, 15, 4.59, 2.96, 0.305)
+    pos, species, cell = rutile_positions(cells[0], cells[1], cells[2], 4.59, 2.96, 0.305)
     pos = pos + rng.normal(0.0, 0.1, pos.shape)
     funcs = behler_functions(types)
     setups = {t: nnfile.behler_setup(t, types, funcs, RC_MIN) for t in types}

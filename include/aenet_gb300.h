@@ -146,7 +146,7 @@ int aenet_gpu_plan_descriptors(aenet_gpu_plan* plan, const void** d_G,
  * CUDA graph, plugins whose host owns the memory pool -- this computes the
  * energy and forces of ONE periodic structure using only the caller's
  * device buffers plus a fixed scratch array compiled into the library
- * (about 19 MB per GPU, held until the process exits).
+ * (about 19.3 MiB per GPU, held until the process exits).
  *
  * Inputs (device): d_coords[3*natoms] Cartesian, d_types[natoms] 1-based;
  * lattice[9] (HOST) rows = lattice vectors.  Outputs (device, any may be

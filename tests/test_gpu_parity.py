@@ -372,3 +372,71 @@ def test_fp32_and_fp64_plans_find_the_same_neighbours(cuda, oracle, tmp_path):
         assert torch.equal(counts[0], counts[1])
     finally:
         ann.release()
+
+
+def test_k3_cu_dimer_scan_on_gpu(cuda, tmp_path):
+    """unittests/Cu-dimer-forces on the GPU: 81 isolated dimers, Behler G2/G4
+    with 16-record (legacy) setups; energies and forces at the printed
+    precision of the reference's output files."""
+    from aenet_gb300.core import FP64
+    k3 = fixtures.load("k3_cu_dimer.npz")
+    pots = fixtures.potentials(k3)
+    paths = fixtures.write_potential_files(pots, str(tmp_path))
+    types = [str(t) for t in k3["types"]]
+    ann = _ann(paths, types)
+    cu = types.index("Cu") + 1
+    try:
+        for x, F, ec, et in zip(k3["positions"], k3["forces"], k3["E_coh"], k3["E_total"]):
+            r = ann.structure_energy_forces(x, np.array([cu, cu], dtype=np.int32), None,
+                                            pbc=False, precision=FP64)
+            assert abs(r["cohesive_energy"] - ec) <= 5.1e-9
+            assert abs(r["energy"] - et) <= 5.1e-9
+            assert np.abs(r["forces"] - F).max() <= 5.1e-7
+    finally:
+        ann.release()
+
+
+@pytest.fixture(scope="module")
+def rutile(oracle, tmp_path_factory):
+    from aenet_gb300 import workloads
+    w = workloads.tio2_rutile_9000(cells=(2, 2, 3))
+    d = tmp_path_factory.mktemp("rutile")
+    paths = helpers.make_potentials(oracle, w, str(d))
+    return w, paths
+
+
+def test_rutile_behler_fp64_parity_virial_and_mixed(cuda, oracle, rutile):
+    from aenet_gb300.core import FP64, MIXED
+    w, paths = rutile
+    s = w.structures[0]
+    ann = _ann(paths, w.types)
+    try:
+        r64 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64,
+                                          virial=True)
+        r32 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=MIXED,
+                                          virial=True)
+    finally:
+        ann.release()
+    oracle.load(w.types, paths)
+    ec, et, F, Ea = oracle.structure(s.cell, s.positions, s.types)
+    n = s.natoms
+    assert abs(r64["energy"] - et) / n < E_TOL_FP64
+    assert np.abs(r64["atomic_energies"] - Ea).max() < E_TOL_FP64
+    assert np.abs(r64["forces"] - F).max() < F_TOL_FP64
+    # virial against central differences of the oracle energy under strain
+    h = 1e-5
+    W = np.zeros((3, 3))
+    for a in range(3):
+        for b in range(3):
+            E = []
+            for sgn in (-1, 1):
+                eps = np.eye(3)
+                eps[a, b] += sgn * h
+                E.append(oracle.structure(s.cell @ eps, s.positions @ eps, s.types,
+                                          forces=False)[1])
+            W[a, b] = -(E[1] - E[0]) / (2 * h)
+    assert np.abs(r64["virial"] - W).max() < 1e-5 * max(1.0, np.abs(W).max())
+    # mixed precision against FP64
+    assert abs(r32["energy"] - r64["energy"]) / n < E_TOL_MIXED
+    dF = r32["forces"] - r64["forces"]
+    assert np.sqrt(np.mean(dF ** 2)) < F_RMS_MIXED
