@@ -93,6 +93,17 @@ def _declare(lib):
     lib.aenet_gpu_structure_energy_forces_noalloc.argtypes = [C.c_int, vp, vp, vp, C.c_int, vp, vp,
                                                               vp, vp, vp]
     lib.aenet_gpu_structure_energy_forces_noalloc.restype = C.c_int
+    lib.aenet_gpu_plan_loss_gradient.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_double,
+                                                 C.c_double, vp, vp, vp, vp, vp]
+    lib.aenet_gpu_plan_loss_gradient.restype = C.c_int
+    lib.aenet_gpu_network_nweights.argtypes = [C.c_int]
+    lib.aenet_gpu_network_nweights.restype = C.c_int
+    lib.aenet_gpu_get_weights.argtypes = [vp]
+    lib.aenet_gpu_get_weights.restype = C.c_int
+    lib.aenet_gpu_set_weights.argtypes = [vp]
+    lib.aenet_gpu_set_weights.restype = C.c_int
+    lib.aenet_gpu_save_potential.argtypes = [C.c_int, C.c_char_p]
+    lib.aenet_gpu_save_potential.restype = C.c_int
     return lib
 
 
@@ -123,3 +134,11 @@ def exported_symbols():
             names.append(m.group(1))
     return sorted(set(n for n in names
                        if not (n.startswith("AENET_GPU_") or n.startswith("AENET_NOALLOC_"))))
+
+
+def ntypes():
+    """Number of loaded species (0 when nothing is loaded)."""
+    n = 0
+    while n < 8 and lib().aenet_gpu_network_nweights(n + 1) >= 0:
+        n += 1
+    return n

@@ -126,6 +126,31 @@ class ANNPotentials:
             raise IOError("File not found: %s" % (filename,))
         check_status(stat.value)
 
+    # ---- network weights (training) ----------------------------------
+    def nweights(self, atom_type=None):
+        """Wsize of one species, or of all species together."""
+        lib = _lib.lib()
+        if atom_type is not None:
+            return lib.aenet_gpu_network_nweights(self.get_type_id(atom_type))
+        return sum(lib.aenet_gpu_network_nweights(t) for t in range(1, self.ntypes + 1))
+
+    def get_weights(self):
+        """All weights: species in type order, each the network's W(1:Wsize)."""
+        W = np.empty(self.nweights(), dtype=np.float64)
+        check_status(_lib.lib().aenet_gpu_get_weights(W.ctypes.data_as(C.c_void_p)))
+        return W
+
+    def set_weights(self, W):
+        W = np.ascontiguousarray(W, dtype=np.float64).reshape(-1)
+        if W.size != self.nweights():
+            raise ValueError("expected %d weights, got %d" % (self.nweights(), W.size))
+        check_status(_lib.lib().aenet_gpu_set_weights(W.ctypes.data_as(C.c_void_p)))
+
+    def save_potential(self, atom_type, filename):
+        """Write the species' potential with its current weights (.nn)."""
+        check_status(_lib.lib().aenet_gpu_save_potential(self.get_type_id(atom_type),
+                                                         str(filename).encode()))
+
     def print_info_to_stdout(self):
         _lib.lib().aenet_print_info()
 

@@ -14,6 +14,7 @@
 // the unfused operations of geo_recip_lattice (geometry.f90:491-516) so
 // that lattice coordinates, and therefore neighbour sets, match the
 // reference bit for bit.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -81,6 +82,7 @@ struct HostPot {
   HostTs ts;
   double E_scale = 1, E_shift = 0, E_atom = 0;
   std::string path;
+  std::vector<std::string> recs;     // the file's records (W is record 9)
 };
 
 std::string trim(const std::string& s) {
@@ -226,9 +228,25 @@ int load_nn(const char* path, const std::vector<std::string>& global_types, Host
   if (it < 0) return 3;
   pot.E_atom = ts.E_atom[it];
   pot.path = path;
+  pot.recs = std::move(r);
   (void)global_types;
   pot.init = true;
   return 0;
+}
+
+// save_Network / save_Setup / save_TrnSet_info in the layout the file was
+// read with, with the current weights in record 9
+bool write_records(const char* path, const std::vector<std::string>& recs) {
+  FILE* f = fopen(path, "wb");
+  if (!f) return false;
+  bool ok = true;
+  for (const auto& r : recs) {
+    int32_t n = (int32_t)r.size();
+    ok = ok && fwrite(&n, 4, 1, f) == 1;
+    ok = ok && (r.empty() || fwrite(r.data(), 1, r.size(), f) == r.size());
+    ok = ok && fwrite(&n, 4, 1, f) == 1;
+  }
+  return fclose(f) == 0 && ok;
 }
 
 // ---------------------------------------------------------------------
@@ -307,6 +325,24 @@ int nmax_nbdist(double rmin, double rmax) {
 
 int odd_pitch(int n) { return (n % 2) ? n : n + 1; }
 
+// Device layout of one network's weights appended to w64: layer l as rows
+// W[o][k] (bias in column nin) with an odd row pitch.  The Fortran slice
+// W(iw+1 : iw+(nin+1)*nout) is column-major (nout, nin+1).
+void device_weights(const HostNet& net, NetTable& nt, std::vector<double>& w64) {
+  int iw = 0;
+  for (int l = 0; l + 1 < net.nlayers; ++l) {
+    int nin = net.nnodes[l], nout = net.nnodes[l + 1];
+    int pitch = odd_pitch(nin + 1);
+    nt.pitch[l] = pitch;
+    nt.w_off[l] = (int)w64.size();
+    size_t base = w64.size();
+    w64.resize(base + (size_t)pitch * nout, 0.0);
+    for (int o = 0; o < nout; ++o)
+      for (int c = 0; c <= nin; ++c) w64[base + (size_t)o * pitch + c] = net.W[iw + o + c * nout];
+    iw += (nin + 1) * nout;
+  }
+}
+
 // Behler tables: registration under the GLOBAL type index and evaluation
 // with the LOCAL (env) index of the central atom's setup, as in
 // setup_symmfunc_Behler2011 (sfsetup.f90:1298) and stp_eval
@@ -360,19 +396,7 @@ int build_device_tables() {
     if (net.nnodes[0] != p.stp.nsf) return AENET_ERR_INPUT;
     nt.f_a[0] = 0;
     for (int l = 1; l < net.nlayers; ++l) nt.f_a[l] = net.f_a[l - 1];
-    int iw = 0;
-    for (int l = 0; l + 1 < net.nlayers; ++l) {
-      int nin = net.nnodes[l], nout = net.nnodes[l + 1];
-      int pitch = odd_pitch(nin + 1);
-      nt.pitch[l] = pitch;
-      nt.w_off[l] = (int)w64.size();
-      size_t base = w64.size();
-      w64.resize(base + (size_t)pitch * nout, 0.0);
-      // Fortran W(iw+1 : iw+(nin+1)*nout) is column-major (nout, nin+1)
-      for (int o = 0; o < nout; ++o)
-        for (int c = 0; c <= nin; ++c) w64[base + (size_t)o * pitch + c] = net.W[iw + o + c * nout];
-      iw += (nin + 1) * nout;
-    }
+    device_weights(net, nt, w64);
     // Chebyshev (setup_basis_chebyshev, sfsetup.f90:1162-1179)
     if (sftype == "chebyshev") {
       sp.sftype = AE_SF_CHEBYSHEV;
@@ -669,8 +693,18 @@ struct aenet_gpu_plan {
   double* E_struct = nullptr;
   double* virial = nullptr;
   unsigned* status = nullptr;
+  // training workspace, allocated by the first loss/gradient call
+  void* tmem = nullptr;
+  int* order = nullptr;       // atoms grouped by species
+  int* spec_off = nullptr;    // [AE_MAXT + 1]
+  int* part_scratch = nullptr;
+  double* cE = nullptr;       // [nstruc] dL/dE coefficients
+  double* loss_s = nullptr;   // [nstruc]
+  void* U = nullptr;          // [N] T4 dL/dF
+  double* partial = nullptr;  // per-block weight-gradient rows
   ~aenet_gpu_plan() {
     if (mem) cudaFree(mem);
+    if (tmem) cudaFree(tmem);
   }
 };
 
@@ -1724,6 +1758,150 @@ EXPORT int aenet_gpu_plan_backward(aenet_gpu_plan* P, const double* d_weights, d
   if (!P) return AENET_ERR_INPUT;
   // the adjoint accumulates forces -dE/dR; the output is their negative
   return plan_adjoint(P, d_weights, d_grad, -1.0, d_virial, (cudaStream_t)stream);
+}
+
+namespace {
+int plan_train_alloc(aenet_gpu_plan* P) {
+  if (P->tmem) return 0;
+  const PotDevice& pd = *P->pd;
+  const size_t N = (size_t)P->natoms, tsz = P->fp64 ? 8 : 4;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = (off + bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  size_t o_ord = take(4 * N);
+  size_t o_so = take(4 * (AE_MAXT + 1));
+  size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(P->natoms));
+  size_t o_ce = take(8 * (size_t)P->nstruc);
+  size_t o_ls = take(8 * (size_t)P->nstruc);
+  size_t o_u = take(4 * tsz * N);
+  size_t o_p = take(8 * (size_t)pd.ntypes * ae_wgrad_nblk() * ae_wgrad_wcap(pd));
+  if (cudaMalloc(&P->tmem, off) != cudaSuccess) {
+    P->tmem = nullptr;
+    return AENET_ERR_CUDA;
+  }
+  char* b = (char*)P->tmem;
+  P->order = (int*)(b + o_ord);
+  P->spec_off = (int*)(b + o_so);
+  P->part_scratch = (int*)(b + o_ps);
+  P->cE = (double*)(b + o_ce);
+  P->loss_s = (double*)(b + o_ls);
+  P->U = (void*)(b + o_u);
+  P->partial = (double*)(b + o_p);
+  if (cudaMemset(P->tmem, 0, off) != cudaSuccess) return AENET_ERR_CUDA;
+  return 0;
+}
+}  // namespace
+
+// Loss and gradient with respect to every network weight (training).
+EXPORT int aenet_gpu_plan_loss_gradient(aenet_gpu_plan* P, const double* d_coords,
+                                        const int* d_types, const double* d_E_target,
+                                        const double* d_F_target, int mode, double w_E,
+                                        double w_F, double* d_loss, double* d_grad, double* d_E,
+                                        double* d_F, void* stream) {
+  if (!P || !d_coords || !d_types || !d_E_target || !d_loss || !d_grad) return AENET_ERR_INPUT;
+  if (mode != AENET_GPU_LOSS_ENERGY && mode != AENET_GPU_LOSS_ENERGY_FORCES) return AENET_ERR_INPUT;
+  const PotDevice& pd = *P->pd;
+  const bool force_term = mode == AENET_GPU_LOSS_ENERGY_FORCES && w_F != 0.0;
+  if (force_term && !d_F_target) return AENET_ERR_INPUT;
+  // the force term needs the descriptor tangent, written for Chebyshev bases
+  if (force_term && pd.sp[0].sftype != AE_SF_CHEBYSHEV) return AENET_ERR_INPUT;
+  if (mode == AENET_GPU_LOSS_ENERGY)
+    for (int t = 1; t < pd.ntypes; ++t)
+      if (std::fabs(pd.sp[t].E_scale - pd.sp[0].E_scale) > 1e-12 * std::fabs(pd.sp[0].E_scale))
+        return AENET_ERR_INPUT;   // one normalisation for the whole training set
+  int st = plan_train_alloc(P);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  st = plan_forward(P, d_coords, d_types, d_E, nullptr, s);
+  if (st) return st;
+  if (force_term || d_F) {
+    st = plan_adjoint(P, nullptr, d_F, 1.0, nullptr, s);
+    if (st) return st;
+  }
+  if (ck(ae_launch_loss(P->nstruc, P->geom_d, P->E_struct, d_E_target, P->Facc,
+                        force_term ? d_F_target : nullptr, mode == AENET_GPU_LOSS_ENERGY ? 0 : 1, w_E, w_F, pd.sp[0].E_scale, P->cE,
+                        P->U, P->loss_s, d_loss, P->fp64, s)))
+    return AENET_ERR_CUDA;
+  if (force_term) {
+    DescBuffers d = desc_buffers(P, nullptr, false);
+    d.U = P->U;
+    d.V = P->dEdG;   // dE/dG is not needed any more in this pass
+    if (ck(ae_launch_chebyshev_tangent(pd, d, P->fp64, s))) return AENET_ERR_CUDA;
+  }
+  if (ck(ae_launch_partition(P->natoms, pd.ntypes, P->types0, P->part_scratch, P->order,
+                             P->spec_off, s)))
+    return AENET_ERR_CUDA;
+  if (ck(ae_launch_mlp_wgrad(pd, P->order, P->spec_off, P->G, force_term ? P->dEdG : nullptr,
+                             P->atom_struct, P->cE, force_term ? -1.0 : 0.0,
+                             mode == AENET_GPU_LOSS_ENERGY_FORCES, P->partial, d_grad, P->fp64, s)))
+    return AENET_ERR_CUDA;
+  return 0;
+}
+
+// ---- network weights ------------------------------------------------
+
+EXPORT int aenet_gpu_network_nweights(int type_id) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init || type_id < 1 || type_id > g.ntypes || !g.pots[type_id - 1].init) return -1;
+  return g.pots[type_id - 1].net.Wsize;
+}
+
+EXPORT int aenet_gpu_get_weights(double* W) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init || !g.loaded) return AENET_ERR_INIT;
+  if (!W) return AENET_ERR_INPUT;
+  size_t o = 0;
+  for (auto& p : g.pots) {
+    std::copy(p.net.W.begin(), p.net.W.end(), W + o);
+    o += p.net.W.size();
+  }
+  return AENET_OK;
+}
+
+// Replace every species' weights (type order, each W(1:Wsize)).  The device
+// copies are overwritten in place, so plans and captured graphs stay valid.
+EXPORT int aenet_gpu_set_weights(const double* W) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init || !g.loaded) return AENET_ERR_INIT;
+  if (!W) return AENET_ERR_INPUT;
+  size_t total = 0;
+  for (auto& p : g.pots) total += p.net.W.size();
+  for (size_t q = 0; q < total; ++q)
+    if (!std::isfinite(W[q])) return AENET_ERR_INPUT;
+  size_t o = 0;
+  for (auto& p : g.pots) {
+    std::copy(W + o, W + o + p.net.W.size(), p.net.W.begin());
+    if (p.recs.size() > 8 && p.recs[8].size() == 8 * p.net.W.size())
+      memcpy(&p.recs[8][0], p.net.W.data(), 8 * p.net.W.size());
+    o += p.net.W.size();
+  }
+  if (g.dev_ready) {
+    std::vector<double> w64;
+    for (int t = 0; t < g.ntypes; ++t) {
+      NetTable nt{};
+      device_weights(g.pots[t].net, nt, w64);
+    }
+    std::vector<float> w32(w64.begin(), w64.end());
+    if (cudaMemcpy(const_cast<double*>(g.pd.w64), w64.data(), 8 * w64.size(), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(const_cast<float*>(g.pd.w32), w32.data(), 4 * w32.size(), cudaMemcpyHostToDevice))
+      return AENET_ERR_CUDA;
+  }
+  return AENET_OK;
+}
+
+// Write the potential of one species with its current weights, in the
+// record layout it was read with (save_Network / save_Setup /
+// save_TrnSet_info, feedforward.f90:291-306, sfsetup.f90:585-609,
+// trainset.f90:432-441).
+EXPORT int aenet_gpu_save_potential(int type_id, const char* filename) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init) return AENET_ERR_INIT;
+  if (type_id < 1 || type_id > g.ntypes || !g.pots[type_id - 1].init) return AENET_ERR_TYPE;
+  if (!filename || strlen(filename) > 1024) return AENET_ERR_MALLOC;
+  return write_records(filename, g.pots[type_id - 1].recs) ? AENET_OK : AENET_ERR_IO;
 }
 
 // Same pipeline as aenet_gpu_plan_run(..., AENET_GPU_FORCES) with CUDA

@@ -175,11 +175,15 @@ struct DescBuffers {
   const int* atom_struct;
   const double* grad_scale;    // per structure factor on dE (or null = 1)
   unsigned* status;
+  const void* U;               // [N] T4 per-atom directions of the tangent pass
+  void* V;                     // [N][nsf_pad] (T) normalised descriptor tangents
 };
 
 int ae_launch_chebyshev_forward(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);
 int ae_launch_chebyshev_adjoint(const PotDevice& pd, const DescBuffers& b,
+                                int fp64, cudaStream_t s);
+int ae_launch_chebyshev_tangent(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);
 int ae_launch_behler_forward(const PotDevice& pd, const DescBuffers& b,
                              int fp64, cudaStream_t s);
@@ -195,3 +199,17 @@ int ae_launch_energy_reduce(int nstruc, const StructGeom* geom,
                             cudaStream_t s);
 int ae_launch_forces_out(int natoms, const void* Facc, int fp64, double* F,
                          double sign, cudaStream_t s);
+
+// training: species partition, loss, weight gradients (k_train.cu)
+int ae_part_scratch_ints(int natoms);
+int ae_launch_partition(int natoms, int ntypes, const int* types0, int* scratch, int* order,
+                        int* spec_off, cudaStream_t s);
+int ae_launch_loss(int nstruc, const StructGeom* geom, const double* E_struct, const double* E_tgt,
+                   const void* Facc, const double* F_tgt, int mode, double wE, double wF,
+                   double E_scale, double* cE, void* U, double* loss_s, double* loss, int fp64,
+                   cudaStream_t s);
+int ae_wgrad_wcap(const PotDevice& pd);
+int ae_wgrad_nblk();
+int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_off, const void* G,
+                        const void* V, const int* atom_struct, const double* cE, double cF,
+                        int physical, double* partial, double* grad, int fp64, cudaStream_t s);

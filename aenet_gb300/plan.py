@@ -18,6 +18,9 @@ from .core import FP64, MIXED, check_status
 FORCES = 1
 VIRIAL = 2
 
+LOSS_ENERGY = 1
+LOSS_ENERGY_FORCES = 2
+
 ST_NB_OVERFLOW = 1
 ST_BAD_COORD = 2
 ST_BAD_TYPE = 4
@@ -26,6 +29,10 @@ ST_CELL_OVERFLOW = 8
 
 class PlanStatusError(RuntimeError):
     pass
+
+
+def _ntypes():
+    return _lib.ntypes()
 
 
 def _stream():
@@ -142,6 +149,34 @@ class Plan:
                                                 _stream())
         check_status(st)
         return grad
+
+    def loss_gradient(self, pos, types, E_target, F_target=None, mode=None, w_E=1.0, w_F=0.1,
+                      grad=None, loss=None, E=None, F=None):
+        """Loss of the batch and its gradient with respect to every network
+        weight (flattened like :func:`aenet_gb300.core.ANNPotentials.get_weights`).
+
+        mode LOSS_ENERGY: the reference's energy loss (train.f90:799-889);
+        mode LOSS_ENERGY_FORCES: w_E sum (E-E_t)^2/N^2 + w_F sum |F-F_t|^2.
+        Returns (loss[1], grad) as CUDA float64 tensors."""
+        self._check_inputs(pos, types)
+        dev = pos.device
+        lib = _lib.lib()
+        if mode is None:
+            mode = LOSS_ENERGY_FORCES if F_target is not None else LOSS_ENERGY
+        if grad is None:
+            nw = sum(lib.aenet_gpu_network_nweights(t) for t in range(1, _ntypes() + 1))
+            grad = torch.empty(nw, dtype=torch.float64, device=dev)
+        if loss is None:
+            loss = torch.empty(1, dtype=torch.float64, device=dev)
+        E_target = E_target.to(device=dev, dtype=torch.float64).contiguous()
+        if F_target is not None:
+            F_target = F_target.to(device=dev, dtype=torch.float64).contiguous()
+        st = lib.aenet_gpu_plan_loss_gradient(self._h, _p(pos), _p(types), _p(E_target),
+                                              _p(F_target), int(mode), float(w_E), float(w_F),
+                                              _p(loss), _p(grad), _p(E), _p(F), _stream())
+        check_status(st)
+        self.generation += 1
+        return loss, grad
 
     STAGES = ("types", "neighbours", "descriptor", "networks", "energy_reduce", "adjoint",
               "forces_out")

@@ -1,0 +1,88 @@
+"""Training of the network weights on the GPU.
+
+Replaces the optimisation loop of train.x: per epoch, eval_next_structure
+for every structure (src/train.f90:799-889) accumulates the loss and the
+weight gradient, and opt_bfgs_weights (src/optimize.f90:1721-1771) takes one
+L-BFGS-B step over the flattened weights of all species.  Here the loss and
+gradient of the whole training set come from one GPU pass
+(``aenet_gpu_plan_loss_gradient``: neighbours, descriptors, networks,
+forces, descriptor tangents and weight gradients), and the optimiser is
+L-BFGS-B with m = 20 correction pairs and no bounds, as opt_init_bfgs sets
+it up (src/optimize.f90:1600-1609).  The reference links L-BFGS-B 3.0
+(lib/Lbfgsb.3.0, Byrd, Lu, Nocedal and Zhu); scipy.optimize ships an
+implementation of the same algorithm, used here on the host -- it handles a
+vector of a few thousand weights per step, negligible next to the GPU pass.
+
+Two losses (``mode``):
+  LOSS_ENERGY         the reference's: sum_s dE_s^2/2 with
+                      dE_s = (E_t,s - E_s)/(E_scale N_s);
+  LOSS_ENERGY_FORCES  w_E sum_s (E_s - E_t,s)^2/N_s^2 + w_F sum_i |F_i - F_t,i|^2.
+"""
+import numpy as np
+import torch
+
+from .core import FP64
+from .plan import LOSS_ENERGY, LOSS_ENERGY_FORCES, Plan
+
+__all__ = ["Trainer", "LOSS_ENERGY", "LOSS_ENERGY_FORCES"]
+
+
+class Trainer:
+    """Loss, gradient and L-BFGS-B fit of the loaded potentials on a fixed
+    training set held in device memory.
+
+    ``structures``: sequence of (positions (N, 3), type ids (N,) 1-based,
+    cell (3, 3) or None, pbc).  ``E_target``: total energies (eV) per
+    structure; ``F_target``: forces (sum N, 3) in eV/A (LOSS_ENERGY_FORCES).
+    """
+
+    def __init__(self, potentials, structures, E_target, F_target=None, mode=None, w_E=1.0,
+                 w_F=0.1, precision=FP64):
+        self.pot = potentials
+        structures = list(structures)
+        natoms = [len(s[1]) for s in structures]
+        cells = np.stack([np.eye(3) if s[2] is None else np.asarray(s[2], dtype=np.float64)
+                          for s in structures])
+        pbc = np.array([1 if s[3] else 0 for s in structures], dtype=np.int32)
+        pos = np.concatenate([np.asarray(s[0], dtype=np.float64).reshape(-1, 3)
+                              for s in structures])
+        types = np.concatenate([np.asarray(s[1], dtype=np.int32) for s in structures])
+        self.mode = mode if mode is not None else (
+            LOSS_ENERGY_FORCES if F_target is not None else LOSS_ENERGY)
+        self.w_E, self.w_F = float(w_E), float(w_F)
+        self.plan = Plan(natoms, cells, pbc, precision=precision,
+                         coords0=None if pbc.all() else pos)
+        dev = torch.device("cuda")
+        self.pos = torch.as_tensor(pos, device=dev).contiguous()
+        self.types = torch.as_tensor(types, device=dev).contiguous()
+        self.E_t = torch.as_tensor(np.asarray(E_target, dtype=np.float64), device=dev).contiguous()
+        self.F_t = None if F_target is None else torch.as_tensor(
+            np.asarray(F_target, dtype=np.float64).reshape(-1, 3), device=dev).contiguous()
+        self.nw = potentials.nweights()
+        self.grad = torch.empty(self.nw, dtype=torch.float64, device=dev)
+        self.loss = torch.empty(1, dtype=torch.float64, device=dev)
+        self.evaluations = 0
+
+    def loss_and_grad(self, W=None):
+        """(loss, gradient) at the weights W (the current ones if None)."""
+        if W is not None:
+            self.pot.set_weights(W)
+        self.plan.loss_gradient(self.pos, self.types, self.E_t, self.F_t, mode=self.mode,
+                                w_E=self.w_E, w_F=self.w_F, grad=self.grad, loss=self.loss)
+        self.plan.check()
+        self.evaluations += 1
+        return float(self.loss.item()), self.grad.cpu().numpy().copy()
+
+    def fit(self, maxiter=100, m=20, gtol=0.0, ftol=0.0, callback=None):
+        """L-BFGS-B over all weights; leaves the best weights loaded and
+        returns scipy's OptimizeResult."""
+        from scipy.optimize import minimize
+        x0 = self.pot.get_weights()
+        res = minimize(self.loss_and_grad, x0, jac=True, method="L-BFGS-B", callback=callback,
+                       options={"maxcor": int(m), "maxiter": int(maxiter), "gtol": gtol,
+                                "ftol": ftol})
+        self.pot.set_weights(res.x)
+        return res
+
+    def close(self):
+        self.plan.close()

@@ -138,6 +138,48 @@ int aenet_gpu_plan_neighbors(aenet_gpu_plan* plan, int* cap,
 int aenet_gpu_plan_descriptors(aenet_gpu_plan* plan, const void** d_G,
                                int* nsf_pad);
 
+/* ---- training ---------------------------------------------------------
+ * Loss of a batch against target energies (and forces) and its gradient
+ * with respect to every network weight, in one stream-ordered pass.
+ * Replaces eval_next_structure / eval_net (src/train.f90:799-916) with
+ * ff_wderiv (src/ext/feedforward.f90:763-860) and the accumulation of
+ * src/optimize.f90:698-734.
+ *
+ * mode AENET_GPU_LOSS_ENERGY: the reference's loss,
+ *     SSE = sum_s dE_s^2 / 2,  dE_s = (E_target,s - E_s) / (E_scale N_s),
+ *     gradient sum_s dE_s Dw_s, Dw_s = -sum_{i in s} dy_i/dw / N_s
+ *     (y: network output in normalised units; w_E, w_F ignored; every
+ *     species must share E_scale, as potentials trained together do).
+ * mode AENET_GPU_LOSS_ENERGY_FORCES (no counterpart in the reference,
+ *     whose force training is not implemented, train.f90:812-813):
+ *     L = w_E sum_s (E_s - E_target,s)^2 / N_s^2
+ *       + w_F sum_i |F_i - F_target,i|^2   (eV, Angstrom);
+ *     the force term is differentiated exactly (Chebyshev bases only).
+ * Device arrays: d_E_target[nstruc] total energies, d_F_target[3N] (mode
+ * 2 with w_F != 0), *d_loss, d_grad[sum over species of Wsize] ordered
+ * like aenet_gpu_get_weights; d_E[nstruc] and d_F[3N] (optional) receive
+ * the energies and forces of the same pass. */
+#define AENET_GPU_LOSS_ENERGY 1
+#define AENET_GPU_LOSS_ENERGY_FORCES 2
+int aenet_gpu_plan_loss_gradient(aenet_gpu_plan* plan, const double* d_coords,
+                                 const int* d_types, const double* d_E_target,
+                                 const double* d_F_target, int mode, double w_E,
+                                 double w_F, double* d_loss, double* d_grad,
+                                 double* d_E, double* d_F, void* stream);
+
+/* Network weights of all species, concatenated in type order, each the
+ * reference's W(1:Wsize) (src/ext/feedforward.f90:55-89, the order
+ * opt_bfgs_weights flattens them in, src/optimize.f90:1731-1737).
+ * aenet_gpu_network_nweights returns Wsize of one species (-1 if not
+ * loaded).  aenet_gpu_set_weights updates the device copies in place:
+ * existing plans and captured graphs use the new weights. */
+int aenet_gpu_network_nweights(int type_id);
+int aenet_gpu_get_weights(double* W);
+int aenet_gpu_set_weights(const double* W);
+/* Write one species' potential with its current weights (.nn, the record
+ * layout it was read with). */
+int aenet_gpu_save_potential(int type_id, const char* filename);
+
 /* ---- evaluation without device memory allocation ---------------------
  * No counterpart in the reference (aenet runs on the CPU and allocates its
  * work arrays per call).  For callers that cannot allocate device memory

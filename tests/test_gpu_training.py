@@ -1,0 +1,187 @@
+"""Loss and weight gradients on the GPU (training), against the oracle.
+
+Energy loss (the reference's, src/train.f90:799-889 + optimize.f90:698-734):
+the FP64 GPU gradient equals sum_s dE_s Dw_s assembled from the oracle's
+per-atom ff_wderiv restatement, to 1e-10 relative.
+Energy + force loss (no reference counterpart): FP64 gradient against
+central differences of the FP64 GPU loss (Richardson, relative 1e-6);
+mixed-precision gradient against FP64 (relative 2e-3 of the norm).
+"""
+import numpy as np
+import pytest
+
+from tests import helpers
+
+pytestmark = pytest.mark.gpu
+
+G_REL_FP64 = 1e-10
+G_REL_FD = 1e-6
+G_REL_MIXED = 2e-3
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def batch(oracle, tmp_path_factory):
+    """Eight small Li/Si/O cells (many periodic images) with targets from a
+    teacher network of the same architecture and another seed."""
+    from aenet_gb300 import workloads
+    w = workloads.lisio_batch_4096(nstruc=8)
+    d = tmp_path_factory.mktemp("train")
+    paths = helpers.make_potentials(oracle, w, str(d))
+    rng = np.random.default_rng(104)
+    teacher = workloads.glorot_networks(rng, w.types, w.arch)
+    tpaths = workloads.write_potentials(w, str(d / "teacher"), stats=_stats_of(paths, w),
+                                        networks=teacher)
+    return w, paths, tpaths
+
+
+def _stats_of(paths, w):
+    from aenet_gb300.nnfile import read_nn
+    out = {}
+    for t in w.types:
+        _, stp, _, _ = read_nn(paths[t])
+        out[t] = (stp["sfval_min"], stp["sfval_max"], stp["sfval_avg"], stp["sfval_cov"])
+    return out
+
+
+def _ann(paths, types):
+    from aenet_gb300.core import ANNPotentials
+    return ANNPotentials({t: paths[t] for t in types}, angular_domain="current")
+
+
+def _structs(w):
+    return [(s.positions, s.types, s.cell, True) for s in w.structures]
+
+
+def _targets(w, tpaths):
+    from aenet_gb300.core import FP64
+    ann = _ann(tpaths, w.types)
+    try:
+        r = ann.batch_energy_forces(_structs(w), precision=FP64)
+    finally:
+        ann.release()
+    return r["energy"], r["forces"]
+
+
+def test_energy_loss_gradient_matches_oracle(cuda, oracle, batch):
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64
+    from aenet_gb300.train import LOSS_ENERGY, Trainer
+    w, paths, tpaths = batch
+    E_t, _ = _targets(w, tpaths)
+    ann = _ann(paths, w.types)
+    try:
+        tr = Trainer(ann, _structs(w), E_t, mode=LOSS_ENERGY, precision=FP64)
+        loss, g = tr.loss_and_grad()
+        loss2, g2 = tr.loss_and_grad()
+        nws = [ann.nweights(t) for t in w.types]
+        tr.close()
+    finally:
+        ann.release()
+    # the reduction of the weight gradient is order-fixed; the forces and
+    # the cell lists upstream use atomics, so reruns agree to rounding
+    assert abs(loss - loss2) <= 1e-12 * loss
+    assert np.abs(g - g2).max() <= 1e-10 * np.abs(g).max()
+    # oracle: per structure dE_s and Dw_s from per-atom ff_wderiv
+    oracle.load(w.types, paths)
+    offs = np.concatenate([[0], np.cumsum(nws)])
+    ref = np.zeros(offs[-1])
+    sse = 0.0
+    for k, s in enumerate(w.structures):
+        _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types)
+        E = 0.0
+        Dw = np.zeros_like(ref)
+        for a in range(s.natoms):
+            nbcoo, _, _, nbt = nb[a]
+            t = int(s.types[a])
+            Ei, gi = oracle.atomic_energy_wgrad(centres[a], t, nbcoo, nbt)
+            E += Ei
+            Dw[offs[t - 1]:offs[t]] -= gi / s.natoms
+        E_scale = 1.0 / workloads.TS_SCALE
+        dE = (E_t[k] - E) / (E_scale * s.natoms)
+        sse += 0.5 * dE * dE
+        ref += dE * Dw / E_scale
+    assert abs(loss - sse) <= G_REL_FP64 * max(sse, 1e-30) + 1e-18
+    assert np.abs(g - ref).max() <= G_REL_FP64 * np.abs(ref).max()
+
+
+def test_force_loss_gradient_matches_finite_differences(cuda, batch):
+    from aenet_gb300.core import FP64
+    from aenet_gb300.train import LOSS_ENERGY_FORCES, Trainer
+    w, paths, tpaths = batch
+    E_t, F_t = _targets(w, tpaths)
+    ann = _ann(paths, w.types)
+    try:
+        tr = Trainer(ann, _structs(w), E_t, F_t, mode=LOSS_ENERGY_FORCES, w_E=1.0, w_F=0.1,
+                     precision=FP64)
+        W0 = ann.get_weights()
+        loss, g = tr.loss_and_grad()
+        nws = [ann.nweights(t) for t in w.types]
+        offs = np.concatenate([[0], np.cumsum(nws)])
+        # per species: a first-layer weight, a first-layer bias, a hidden
+        # weight and the output bias
+        picks = []
+        for t in range(len(w.types)):
+            o = offs[t]
+            picks += [o + 5, o + 32 * 32 + 7, o + 33 * 32 + 40, offs[t + 1] - 1]
+        for k in picks:
+            h = 1e-4 * max(1.0, abs(W0[k]))
+            f = {}
+            for m in (-2, -1, 1, 2):
+                Wm = W0.copy()
+                Wm[k] += m * h
+                f[m] = tr.loss_and_grad(Wm)[0]
+            fd = (8 * (f[1] - f[-1]) - (f[2] - f[-2])) / (12 * h)
+            assert abs(fd - g[k]) <= G_REL_FD * max(abs(g[k]), 1e-3 * np.abs(g).max()), (k, fd, g[k])
+        tr.loss_and_grad(W0)
+        tr.close()
+    finally:
+        ann.release()
+
+
+def test_mixed_gradient_close_to_fp64(cuda, batch):
+    from aenet_gb300.core import FP64, MIXED
+    from aenet_gb300.train import LOSS_ENERGY_FORCES, Trainer
+    w, paths, tpaths = batch
+    E_t, F_t = _targets(w, tpaths)
+    ann = _ann(paths, w.types)
+    try:
+        out = {}
+        for prec in (FP64, MIXED):
+            tr = Trainer(ann, _structs(w), E_t, F_t, mode=LOSS_ENERGY_FORCES, precision=prec)
+            out[prec] = tr.loss_and_grad()
+            tr.close()
+    finally:
+        ann.release()
+    (l64, g64), (l32, g32) = out[FP64], out[MIXED]
+    assert abs(l32 - l64) <= G_REL_MIXED * l64
+    assert np.linalg.norm(g32 - g64) <= G_REL_MIXED * np.linalg.norm(g64)
+
+
+def test_lbfgs_fit_reduces_loss_and_saves_weights(cuda, batch, tmp_path):
+    from aenet_gb300.core import MIXED
+    from aenet_gb300.nnfile import read_nn
+    from aenet_gb300.train import LOSS_ENERGY_FORCES, Trainer
+    w, paths, tpaths = batch
+    E_t, F_t = _targets(w, tpaths)
+    ann = _ann(paths, w.types)
+    try:
+        tr = Trainer(ann, _structs(w), E_t, F_t, mode=LOSS_ENERGY_FORCES, precision=MIXED)
+        l0, _ = tr.loss_and_grad()
+        res = tr.fit(maxiter=25)
+        l1, _ = tr.loss_and_grad()
+        tr.close()
+        assert l1 < 0.5 * l0, (l0, l1, res.message)
+        W = ann.get_weights()
+        ann.save_potential(w.types[0], tmp_path / "saved.nn")
+        net, _, _, _ = read_nn(str(tmp_path / "saved.nn"))
+        assert np.array_equal(net["W"], W[:ann.nweights(w.types[0])])
+    finally:
+        ann.release()

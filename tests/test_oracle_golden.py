@@ -122,3 +122,40 @@ def test_cell_search_as_written_is_complete_on_small_cells(oracle):
             sets.append([sorted(zip(x[2].tolist(), map(tuple, x[0].tolist()))) for x in nb])
         oracle.set_candidates("complete")
         assert sets[0] == sets[1]
+
+
+def test_oracle_weight_gradient_matches_finite_differences(oracle, k1, tmp_path):
+    """ff_wderiv restatement (feedforward.f90:763-860) against central
+    differences of the atomic energy with respect to single weights of the
+    K-1 Ti network (44-15-15-1): hidden-layer weights, biases and the
+    output layer."""
+    import copy
+    pots = fixtures.potentials(k1)
+    paths = fixtures.write_potential_files(pots, str(tmp_path))
+    oracle.load(["Ti", "O"], paths, angular="legacy")
+    types = _types(k1, k1["symbols"])
+    _, centres, nb = oracle.neighbors(k1["cell"], k1["positions"], types, atoms=[0])
+    nbcoo, _, _, nbt = nb[0]
+    E0, g = oracle.atomic_energy_wgrad(centres[0], int(types[0]), nbcoo, nbt)
+    assert abs(E0 - oracle.atomic_energy(centres[0], int(types[0]), nbcoo, nbt)) < 1e-12
+    W = np.array(pots["Ti"]["net"]["W"], dtype=np.float64)
+    nw = W.size
+    # first layer (weight, bias), second layer, output weight and bias
+    picks = [0, 7, 44 * 15 + 3, 45 * 15 + 2, 45 * 15 + 16 * 15 - 1, nw - 2, nw - 1]
+
+    def energy(w):
+        p = copy.deepcopy(pots)
+        p["Ti"]["net"]["W"] = w
+        ps = fixtures.write_potential_files(p, str(tmp_path))
+        oracle.load(["Ti", "O"], ps, angular="legacy")
+        return oracle.atomic_energy(centres[0], int(types[0]), nbcoo, nbt)
+
+    for k in picks:
+        h = 1e-4 * max(1.0, abs(W[k]))
+        f = {}
+        for m in (-2, -1, 1, 2):
+            w = W.copy()
+            w[k] += m * h
+            f[m] = energy(w)
+        fd = (8 * (f[1] - f[-1]) - (f[2] - f[-2])) / (12 * h)
+        assert abs(fd - g[k]) <= 1e-7 * max(1.0, abs(g[k])), (k, fd, g[k])
