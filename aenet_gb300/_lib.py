@@ -104,6 +104,19 @@ def _declare(lib):
     lib.aenet_gpu_set_weights.restype = C.c_int
     lib.aenet_gpu_save_potential.argtypes = [C.c_int, C.c_char_p]
     lib.aenet_gpu_save_potential.restype = C.c_int
+    lib.aenet_gpu_md_create.argtypes = [C.c_int, vp, vp, vp, vp, vp, C.c_double, C.c_double,
+                                        C.c_int, ip]
+    lib.aenet_gpu_md_create.restype = vp
+    lib.aenet_gpu_md_destroy.argtypes = [vp]
+    lib.aenet_gpu_md_destroy.restype = None
+    lib.aenet_gpu_md_run.argtypes = [vp, C.c_int, dp, dp]
+    lib.aenet_gpu_md_run.restype = C.c_int
+    lib.aenet_gpu_md_get.argtypes = [vp, vp, vp, vp]
+    lib.aenet_gpu_md_get.restype = C.c_int
+    lib.aenet_gpu_md_counters.argtypes = [vp, C.POINTER(C.c_longlong), ip]
+    lib.aenet_gpu_md_counters.restype = C.c_int
+    lib.aenet_gpu_md_energy_fp64.argtypes = [vp, dp]
+    lib.aenet_gpu_md_energy_fp64.restype = C.c_int
     return lib
 
 

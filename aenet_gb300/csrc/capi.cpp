@@ -1031,6 +1031,8 @@ NbBuffers nb_buffers(aenet_gpu_plan* P) {
 
 int ck(int e) { return e ? AENET_ERR_CUDA : 0; }
 
+int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s);
+
 // neighbours + descriptors + networks + energies
 int plan_forward(aenet_gpu_plan* P, const double* d_coords, const int* d_types, double* d_E,
                  double* d_E_atoms, cudaStream_t s) {
@@ -1038,6 +1040,12 @@ int plan_forward(aenet_gpu_plan* P, const double* d_coords, const int* d_types, 
   if (ck(ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s))) return AENET_ERR_CUDA;
   NbBuffers nb = nb_buffers(P);
   if (ck(ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s))) return AENET_ERR_CUDA;
+  return plan_eval(P, d_E, d_E_atoms, s);
+}
+
+// descriptors + networks + energies on the current neighbour table
+int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s) {
+  const PotDevice& pd = *P->pd;
   DescBuffers d = desc_buffers(P, nullptr, false);
   int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
                                              : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
@@ -1839,6 +1847,239 @@ EXPORT int aenet_gpu_plan_loss_gradient(aenet_gpu_plan* P, const double* d_coord
                              mode == AENET_GPU_LOSS_ENERGY_FORCES, P->partial, d_grad, P->fp64, s)))
     return AENET_ERR_CUDA;
   return 0;
+}
+
+// ---- molecular dynamics ---------------------------------------------
+
+// amu A^2 / fs^2 in eV: 1.66053906660e-27 kg * 1e10 m^2/s^2 / 1.602176634e-19 J
+static const double MD_MASS_UNIT = 1.66053906660e-17 / 1.602176634e-19;
+
+struct aenet_gpu_md {
+  std::unique_ptr<aenet_gpu_plan> P;
+  std::unique_ptr<aenet_gpu_plan> P64;   // FP64 re-evaluation, created on first use
+  int n = 0, precision = AENET_GPU_MIXED, cap = 0;
+  double dt = 1.0, skin = 0.0;
+  double lattice[9];
+  cudaStream_t stream = nullptr;
+  void* mem = nullptr;
+  double *pos = nullptr, *vel = nullptr, *F = nullptr, *S = nullptr, *rb = nullptr,
+         *invm = nullptr, *part = nullptr, *scal = nullptr;   // scal: E, E_kin, E_fp64
+  int *types = nullptr, *flag = nullptr;
+  long long steps = 0;
+  int builds = 0;
+  ~aenet_gpu_md() {
+    if (mem) cudaFree(mem);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+int md_plan(aenet_gpu_md* M, int cap) {
+  int st = 0;
+  const int pbc = 1;
+  M->P.reset(plan_new(1, &M->n, M->lattice, &pbc, nullptr, M->precision, &g.pd,
+                      aenet_Rc_max + M->skin, cap, true, &st));
+  if (!M->P) return st ? st : AENET_ERR_CUDA;
+  M->cap = M->P->cap;
+  return 0;
+}
+
+// full neighbour search at the current positions, then energies and forces
+int md_build(aenet_gpu_md* M) {
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    aenet_gpu_plan* P = M->P.get();
+    cudaStream_t s = M->stream;
+    if (cudaMemsetAsync(P->status, 0, 4, s)) return AENET_ERR_CUDA;
+    int st = plan_forward(P, M->pos, M->types, nullptr, nullptr, s);
+    if (st) return st;
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, P->status, 4, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
+      return AENET_ERR_CUDA;
+    if (h & (AE_ST_BAD_COORD | AE_ST_BAD_TYPE | AE_ST_CELL_OVERFLOW)) return AENET_ERR_INPUT;
+    if (h & AE_ST_NB_OVERFLOW) {
+      st = md_plan(M, ((M->cap * 3 / 2) + 31) & ~31);
+      if (st) return st;
+      continue;
+    }
+    ++M->builds;
+    if (ck(ae_md_after_build(M->n, M->pos, P->r_wrap, M->S, M->rb, s))) return AENET_ERR_CUDA;
+    return plan_adjoint(P, nullptr, M->F, 1.0, nullptr, s);
+  }
+  return AENET_ERR_MALLOC;
+}
+}  // namespace
+
+// Velocity-Verlet MD of one periodic structure (see include/aenet_gb300.h).
+EXPORT aenet_gpu_md* aenet_gpu_md_create(int natoms, const double* lattice, const double* coords,
+                                         const double* velocities, const int* type_ids,
+                                         const double* masses, double dt, double skin,
+                                         int precision, int* stat) {
+  int dummy;
+  if (!stat) stat = &dummy;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init || !g.loaded) {
+    *stat = AENET_ERR_INIT;
+    return nullptr;
+  }
+  if (natoms < 1 || !lattice || !coords || !type_ids || !masses || !(dt > 0.0) || !(skin >= 0.0) ||
+      (precision != AENET_GPU_FP64 && precision != AENET_GPU_MIXED)) {
+    *stat = AENET_ERR_INPUT;
+    return nullptr;
+  }
+  for (int t = 0; t < g.ntypes; ++t)
+    if (!(masses[t] > 0.0)) {
+      *stat = AENET_ERR_INPUT;
+      return nullptr;
+    }
+  int st = ensure_device();
+  if (st) {
+    *stat = st;
+    return nullptr;
+  }
+  auto M = std::make_unique<aenet_gpu_md>();
+  M->n = natoms;
+  M->dt = dt;
+  M->skin = skin;
+  M->precision = precision;
+  memcpy(M->lattice, lattice, sizeof(M->lattice));
+  if (cudaStreamCreateWithFlags(&M->stream, cudaStreamNonBlocking)) {
+    *stat = AENET_ERR_CUDA;
+    return nullptr;
+  }
+  const size_t N = natoms;
+  const size_t bytes = 8 * (3 * N * 5 + N + ae_md_ekin_blocks() + 4) + 4 * (N + 4) + 256 * 10;
+  if (cudaMalloc(&M->mem, bytes)) {
+    M->mem = nullptr;
+    *stat = AENET_ERR_CUDA;
+    return nullptr;
+  }
+  char* b = (char*)M->mem;
+  size_t off = 0;
+  auto take = [&](size_t n) {
+    char* p = b + off;
+    off = (off + n + 255) & ~(size_t)255;
+    return p;
+  };
+  M->pos = (double*)take(24 * N);
+  M->vel = (double*)take(24 * N);
+  M->F = (double*)take(24 * N);
+  M->S = (double*)take(24 * N);
+  M->rb = (double*)take(24 * N);
+  M->invm = (double*)take(8 * N);
+  M->part = (double*)take(8 * (size_t)ae_md_ekin_blocks());
+  M->scal = (double*)take(32);
+  M->types = (int*)take(4 * N);
+  M->flag = (int*)take(16);
+  std::vector<double> invm(N), v0(3 * N, 0.0);
+  for (size_t i = 0; i < N; ++i) {
+    const int t = type_ids[i];
+    if (t < 1 || t > g.ntypes) {
+      *stat = AENET_ERR_TYPE;
+      return nullptr;
+    }
+    invm[i] = 1.0 / masses[t - 1];
+  }
+  if (velocities) std::copy(velocities, velocities + 3 * N, v0.begin());
+  if (cudaMemcpy(M->pos, coords, 24 * N, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(M->vel, v0.data(), 24 * N, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(M->invm, invm.data(), 8 * N, cudaMemcpyHostToDevice) ||
+      cudaMemcpy(M->types, type_ids, 4 * N, cudaMemcpyHostToDevice)) {
+    *stat = AENET_ERR_CUDA;
+    return nullptr;
+  }
+  st = md_plan(M.get(), 0);
+  if (!st) st = md_build(M.get());
+  if (!st && cudaStreamSynchronize(M->stream)) st = AENET_ERR_CUDA;
+  if (st) {
+    *stat = st;
+    return nullptr;
+  }
+  *stat = AENET_OK;
+  return M.release();
+}
+
+EXPORT void aenet_gpu_md_destroy(aenet_gpu_md* M) { delete M; }
+
+EXPORT int aenet_gpu_md_run(aenet_gpu_md* M, int nsteps, double* E_pot, double* E_kin) {
+  if (!M || nsteps < 0) return AENET_ERR_INPUT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s = M->stream;
+  aenet_gpu_plan* P = M->P.get();
+  const double half_dt_acc = 0.5 * M->dt / MD_MASS_UNIT;
+  const double lim2 = 0.25 * M->skin * M->skin;
+  for (int k = 0; k < nsteps; ++k) {
+    if (ck(ae_md_kick_drift(M->n, M->pos, M->vel, M->F, M->invm, half_dt_acc, M->dt, s)))
+      return AENET_ERR_CUDA;
+    bool rebuild = M->skin <= 0.0;
+    if (!rebuild) {
+      int h = 0;
+      if (ck(ae_md_displacement(M->n, M->pos, M->rb, lim2, M->flag, s)) ||
+          cudaMemcpyAsync(&h, M->flag, 4, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
+        return AENET_ERR_CUDA;
+      rebuild = h != 0;
+    }
+    int st;
+    if (rebuild) {
+      st = md_build(M);
+      P = M->P.get();
+    } else {
+      if (ck(ae_md_refresh(M->n, P->geom_d, P->atom_struct, M->pos, M->S, P->cap, P->nb_cnt,
+                           P->nb_jt, P->nb_img, P->nb_vec, P->fp64, s)))
+        return AENET_ERR_CUDA;
+      st = plan_eval(P, nullptr, nullptr, s);
+      if (!st) st = plan_adjoint(P, nullptr, M->F, 1.0, nullptr, s);
+    }
+    if (st) return st;
+    if (ck(ae_md_kick(M->n, M->vel, M->F, M->invm, half_dt_acc, s))) return AENET_ERR_CUDA;
+    ++M->steps;
+  }
+  if (ck(ae_md_ekin(M->n, M->vel, M->invm, M->part, 0.5 * MD_MASS_UNIT, M->scal + 1, s)) ||
+      cudaMemcpyAsync(M->scal, P->E_struct, 8, cudaMemcpyDeviceToDevice, s))
+    return AENET_ERR_CUDA;
+  double h[2];
+  if (cudaMemcpyAsync(h, M->scal, 16, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
+    return AENET_ERR_CUDA;
+  if (E_pot) *E_pot = h[0];
+  if (E_kin) *E_kin = h[1];
+  return AENET_OK;
+}
+
+EXPORT int aenet_gpu_md_get(aenet_gpu_md* M, double* coords, double* velocities, double* forces) {
+  if (!M) return AENET_ERR_INPUT;
+  const size_t b = 24 * (size_t)M->n;
+  cudaStream_t s = M->stream;
+  if ((coords && cudaMemcpyAsync(coords, M->pos, b, cudaMemcpyDeviceToHost, s)) ||
+      (velocities && cudaMemcpyAsync(velocities, M->vel, b, cudaMemcpyDeviceToHost, s)) ||
+      (forces && cudaMemcpyAsync(forces, M->F, b, cudaMemcpyDeviceToHost, s)) ||
+      cudaStreamSynchronize(s))
+    return AENET_ERR_CUDA;
+  return AENET_OK;
+}
+
+EXPORT int aenet_gpu_md_counters(aenet_gpu_md* M, long long* steps, int* builds) {
+  if (!M) return AENET_ERR_INPUT;
+  if (steps) *steps = M->steps;
+  if (builds) *builds = M->builds;
+  return AENET_OK;
+}
+
+// FP64 energy of the current positions (its own plan without skin)
+EXPORT int aenet_gpu_md_energy_fp64(aenet_gpu_md* M, double* E) {
+  if (!M || !E) return AENET_ERR_INPUT;
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaStream_t s = M->stream;
+  if (!M->P64) {
+    int st = 0;
+    const int pbc = 1;
+    M->P64.reset(plan_new(1, &M->n, M->lattice, &pbc, nullptr, AENET_GPU_FP64, &g.pd, aenet_Rc_max,
+                          0, false, &st));
+    if (!M->P64) return st ? st : AENET_ERR_CUDA;
+  }
+  int st = plan_forward(M->P64.get(), M->pos, M->types, M->scal + 2, nullptr, s);
+  if (st) return st;
+  if (cudaMemcpyAsync(E, M->scal + 2, 8, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
+    return AENET_ERR_CUDA;
+  return AENET_OK;
 }
 
 // ---- network weights ------------------------------------------------

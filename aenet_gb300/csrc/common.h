@@ -213,3 +213,19 @@ int ae_wgrad_nblk();
 int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_off, const void* G,
                         const void* V, const int* atom_struct, const double* cE, double cF,
                         int physical, double* partial, double* grad, int fp64, cudaStream_t s);
+
+// molecular dynamics (k_md.cu)
+int ae_md_kick_drift(int n, double* pos, double* vel, const double* F, const double* invm,
+                     double half_dt_acc, double dt, cudaStream_t s);
+int ae_md_kick(int n, double* vel, const double* F, const double* invm, double half_dt_acc,
+               cudaStream_t s);
+int ae_md_displacement(int n, const double* pos, const double* rb, double lim2, int* flag,
+                       cudaStream_t s);
+int ae_md_after_build(int n, const double* pos, const double* r_wrap, double* S, double* rb,
+                      cudaStream_t s);
+int ae_md_refresh(int n, const StructGeom* geom, const int* atom_struct, const double* pos,
+                  const double* S, int cap, const int* nb_cnt, const int* nb_jt, const int* nb_img,
+                  void* nb_vec, int fp64, cudaStream_t s);
+int ae_md_ekin_blocks();
+int ae_md_ekin(int n, const double* vel, const double* invm, double* part, double half_mass_unit,
+               double* out, cudaStream_t s);

@@ -232,11 +232,8 @@ def cuau_fcc_1m(seed=5, n=64):
                  [Structure(pos, species, cell)], seed)
     w.networks = glorot_networks(rng, types, arch)
     # Maxwell-Boltzmann velocities at 600 K (A/fs), centre of mass removed
-    kB = 8.617333262e-5
-    amu = 1.0364269e-4   # eV fs^2 / A^2
-    m = np.array([MASSES[types[t - 1]] for t in species]) * amu
-    v = rng.normal(0.0, 1.0, pos.shape) * np.sqrt(kB * 600.0 / m)[:, None]
-    v -= (m[:, None] * v).sum(0) / m.sum()
+    from .md import maxwell_boltzmann
+    v = maxwell_boltzmann([MASSES[types[t - 1]] for t in species], 600.0, rng)
     w.velocities = v
     return w
 

@@ -180,6 +180,33 @@ int aenet_gpu_set_weights(const double* W);
  * layout it was read with). */
 int aenet_gpu_save_potential(int type_id, const char* filename);
 
+/* ---- molecular dynamics -------------------------------------------------
+ * Velocity-Verlet NVE dynamics of one periodic structure with the loaded
+ * potentials, every step on the GPU (the integration ASE's VelocityVerlet
+ * performs in python3/scripts/aenet-md.py:72-97, here without ASE and
+ * without a host round trip per step).  Units: coords A, velocities A/fs,
+ * masses[ntypes] amu by type id, dt fs; forces eV/A, energies eV.
+ * Neighbour lists use a Verlet skin: built with Rc + skin and rebuilt when
+ * an atom has moved more than skin/2 (skin 0: rebuilt every step).
+ * precision AENET_GPU_MIXED or AENET_GPU_FP64 (the integration itself is
+ * FP64 in both).  Not thread-safe per object. */
+typedef struct aenet_gpu_md aenet_gpu_md;
+aenet_gpu_md* aenet_gpu_md_create(int natoms, const double* lattice,
+                                  const double* coords, const double* velocities,
+                                  const int* type_ids, const double* masses,
+                                  double dt, double skin, int precision,
+                                  int* stat);
+void aenet_gpu_md_destroy(aenet_gpu_md* md);
+/* nsteps steps; *E_pot, *E_kin (may be NULL) after the last one */
+int aenet_gpu_md_run(aenet_gpu_md* md, int nsteps, double* E_pot, double* E_kin);
+/* host copies of the current state (any may be NULL) */
+int aenet_gpu_md_get(aenet_gpu_md* md, double* coords, double* velocities,
+                     double* forces);
+/* steps taken and neighbour-table builds so far */
+int aenet_gpu_md_counters(aenet_gpu_md* md, long long* steps, int* builds);
+/* plain FP64 energy of the current positions (the mixed run's monitor) */
+int aenet_gpu_md_energy_fp64(aenet_gpu_md* md, double* E);
+
 /* ---- evaluation without device memory allocation ---------------------
  * No counterpart in the reference (aenet runs on the CPU and allocates its
  * work arrays per call).  For callers that cannot allocate device memory
