@@ -61,6 +61,9 @@ def parse():
                     help="fix the descriptor kernels' lanes per atom (implies --no-tune)")
     ap.add_argument("--cell-div", type=int, default=0,
                     help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
+    ap.add_argument("--no-md", action="store_true", help="skip the 1M-atom MD leg")
+    ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "aenet_gb300_bench"))
     return ap.parse_args()
 
@@ -462,7 +465,48 @@ def run_gb300(args):
                          % (len(sample), S, n, threads, dt)}
         o.close()
 
-    launches_per_step = 7
+    # ---- training step on the same batch: loss E + F and its weight gradient
+    train = None
+    if not args.no_train:
+        from aenet_gb300.plan import LOSS_ENERGY_FORCES
+        plan_t = Plan(nat, cells, pbc, precision=MIXED, coords0=pos)
+        E_t = (res32["E"] + 0.01 * natoms_t).contiguous()
+        F_t = (0.9 * res32["F"]).contiguous()
+        gbuf = torch.empty(ann.nweights(), dtype=torch.float64, device=dev)
+        lbuf = torch.empty(1, dtype=torch.float64, device=dev)
+
+        def tstep():
+            plan_t.loss_gradient(p, t, E_t, F_t, mode=LOSS_ENERGY_FORCES, w_E=1.0, w_F=0.1,
+                                 grad=gbuf, loss=lbuf)
+
+        for _ in range(max(1, args.warmup)):
+            tstep()
+        plan_t.check()
+        tms = []
+        for _ in range(max(3, args.steps // 4)):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            tstep()
+            b.record(stream)
+            b.synchronize()
+            tms.append(a.elapsed_time(b))
+        tm = float(np.mean(tms))
+        train = {"workload": "same batch: loss w_E sum (E-E_t)^2/N^2 + w_F sum |F-F_t|^2 and "
+                             "its gradient with respect to all %d weights" % ann.nweights(),
+                 "atoms_per_s": N / (tm * 1e-3), "ms_per_step": tm, "precision": "mixed",
+                 "loss": float(lbuf.item())}
+        plan_t.close()
+
+    md = None
+    if rank == 0 and not args.no_md:
+        ann.release()
+        md = run_md(args, local)
+    else:
+        ann.release()
+
+    launches_per_step = 12   # types, 6 neighbour-search kernels, descriptor, networks,
+    #                          energy reduction, adjoint, force output
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -481,11 +525,57 @@ def run_gb300(args):
                 "errors_vs_fp64": errors, "neighbours": nb,
                 "stages_ms": stages, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+                "train_step": train, "md": md,
                 "wall_s_timed_region": wall}
         print(json.dumps(line), flush=True)
-    ann.release()
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_md(args, local):
+    """1,048,576-atom Cu/Au FCC (25% Au), 100 velocity-Verlet steps of 2 fs
+    from Maxwell-Boltzmann velocities at 600 K, Verlet skin 0.3 A, mixed
+    precision, with the FP64 energy of the same positions every 10 steps."""
+    import torch
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import ANNPotentials, MIXED
+    from aenet_gb300.md import MolecularDynamics
+    w = workloads.cuau_fcc_1m()
+    d = tempfile.mkdtemp(prefix="aenet_md_")
+    paths = workloads.write_potentials(w, d, workloads.gpu_descriptor_fn)
+    ann = ANNPotentials(paths)
+    s = w.structures[0]
+    try:
+        md = MolecularDynamics(ann, s.positions, s.types, s.cell, velocities=w.velocities,
+                               dt=2.0, skin=0.3, precision=MIXED)
+        e0 = md.E_pot + md.E_kin
+        md.run(2)    # warm-up (lazy allocations, first refresh)
+        steps0, builds0 = md.counters()
+        block = 10
+        run_s, monitor, drift = 0.0, [], []
+        for _ in range(max(1, args.md_steps // block)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ep, ek = md.run(block)
+            run_s += time.perf_counter() - t0
+            monitor.append(abs(md.energy_fp64() - ep) / s.natoms)
+            drift.append(abs(ep + ek - e0) / s.natoms)
+        steps, builds = md.counters()
+        nsteps = steps - steps0
+        out = {"workload": "cuau_fcc_1m: 64^3 conventional FCC cells, a = 3.70 A, 25% Au, "
+                           "sigma 0.1 A, Chebyshev r16/6.0 a8/4.0 (52 features), 52-20-20-1 x2",
+               "atoms": s.natoms, "steps": int(nsteps), "dt_fs": 2.0, "skin_A": 0.3,
+               "precision": "mixed forces, fp64 integration",
+               "atom_steps_per_s": s.natoms * nsteps / run_s, "ms_per_step": 1e3 * run_s / nsteps,
+               "neighbour_builds": int(builds - builds0),
+               "fp64_monitor_max_eV_per_atom": max(monitor),
+               "energy_drift_max_eV_per_atom": max(drift),
+               "timing": "host wall clock around md.run blocks of 10 steps (one sync per "
+                         "step for the skin check), FP64 monitor outside"}
+        md.close()
+    finally:
+        ann.release()
+    return out
 
 
 def main():
