@@ -267,6 +267,8 @@ struct State {
   int angular_legacy = 0;
   int cell_div = 2;
   int lpa_default = 16;
+  int networks_tc = 1;       // tensor-core networks on the mixed path when eligible
+  std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
   PotDevice pd{};
@@ -325,6 +327,22 @@ int nmax_nbdist(double rmin, double rmax) {
 
 int odd_pitch(int n) { return (n % 2) ? n : n + 1; }
 
+// BF16 round to nearest even from the FP32 value of v, and back
+uint16_t bf16_rn(double v) {
+  float f = (float)v;
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u) return (uint16_t)(u >> 16);   // inf / nan
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+double bf16_to_double(uint16_t h) {
+  uint32_t u = (uint32_t)h << 16;
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+}
+
 // Device layout of one network's weights appended to w64: layer l as rows
 // W[o][k] (bias in column nin) with an odd row pitch.  The Fortran slice
 // W(iw+1 : iw+(nin+1)*nout) is column-major (nout, nin+1).
@@ -349,6 +367,74 @@ void device_weights(const HostNet& net, NetTable& nt, std::vector<double>& w64) 
 // (sfsetup.f90:925-944); the per-species table below is what
 // sf_fingerprint evaluates for a central atom of that species.
 int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out);
+
+// Split-BF16 images of every species' network for the tensor-core kernel
+// (two hidden layers, input and hidden widths up to 64; TcLayout in
+// common.h).  Sets pd.tc_ok / tc_kin / tc_h; empty when not eligible.
+std::vector<unsigned char> make_tc_image(PotDevice& pd, const std::vector<double>& scale) {
+  std::vector<unsigned char> tc_img;
+  pd.tc_ok = 0;
+  {
+    bool ok = true;
+    int kin = 0, h = 0;
+    for (int t = 0; t < g.ntypes; ++t) {
+      const HostNet& net = g.pots[t].net;
+      if (net.nlayers != 4 || net.nnodes[3] != 1 || net.nnodes[0] > 64 || net.nnodes[1] > 64 ||
+          net.nnodes[2] > 64)
+        ok = false;
+      else {
+        kin = std::max(kin, net.nnodes[0]);
+        h = std::max(h, std::max(net.nnodes[1], net.nnodes[2]));
+      }
+    }
+    if (ok) {
+      kin = kin <= 32 ? 32 : 64;
+      h = h <= 32 ? 32 : 64;
+      const TcLayout L = tc_layout(kin, h);
+      tc_img.assign((size_t)g.ntypes * L.bytes, 0);
+      for (int t = 0; t < g.ntypes; ++t) {
+        const HostNet& net = g.pots[t].net;
+        unsigned char* base = tc_img.data() + (size_t)t * L.bytes;
+        const int n0 = net.nnodes[0], n1 = net.nnodes[1], n2 = net.nnodes[2];
+        const int iw1 = 0, iw2 = (n0 + 1) * n1, iw3 = iw2 + (n1 + 1) * n2;
+        // Fortran W slices are column-major (nout, nin+1), bias in column nin
+        auto W1 = [&](int o, int k) { return net.W[iw1 + o + k * n1]; };
+        auto W2 = [&](int o, int k) { return net.W[iw2 + o + k * n2]; };
+        auto put = [&](int off, int R, int K, int r, int k, double v) {
+          uint16_t hi = bf16_rn(v);
+          uint16_t lo = bf16_rn(v - bf16_to_double(hi));
+          int o = tc_core_offset(r, k, K);
+          memcpy(base + off + o, &hi, 2);
+          memcpy(base + off + 2 * R * K + o, &lo, 2);
+        };
+        for (int o = 0; o < n1; ++o)
+          for (int k = 0; k < n0; ++k) {
+            put(L.b1, h, kin, o, k, W1(o, k));
+            put(L.b1t, kin, h, k, o, W1(o, k));
+          }
+        for (int o = 0; o < n2; ++o)
+          for (int k = 0; k < n1; ++k) {
+            put(L.b2, h, h, o, k, W2(o, k));
+            put(L.b2t, h, h, k, o, W2(o, k));
+          }
+        float* vec = reinterpret_cast<float*>(base + L.vec);
+        for (int o = 0; o < n1; ++o) vec[o] = (float)W1(o, n0);
+        for (int o = 0; o < n2; ++o) vec[h + o] = (float)W2(o, n1);
+        for (int k = 0; k < n2; ++k) vec[2 * h + k] = (float)net.W[iw3 + k];
+        for (int k = 0; k < n0; ++k)
+          vec[3 * h + k] = (float)(pd.sp[t].E_scale * scale[(size_t)t * pd.nsf_pad + k]);
+        vec[3 * h + kin] = (float)net.W[iw3 + n2];
+        vec[3 * h + kin + 1] = (float)net.f_a[0];
+        vec[3 * h + kin + 2] = (float)net.f_a[1];
+        vec[3 * h + kin + 3] = (float)net.f_a[2];
+      }
+      pd.tc_ok = 1;
+      pd.tc_kin = kin;
+      pd.tc_h = h;
+    }
+  }
+  return tc_img;
+}
 
 int build_device_tables() {
   if (!cuda_ok()) return AENET_ERR_CUDA;
@@ -438,6 +524,9 @@ int build_device_tables() {
     shift2[2 * q + 1] = (float)(shift[q] - (double)hi);
     scale32[q] = (float)scale[q];
   }
+  // split-BF16 images for the tensor-core networks
+  std::vector<unsigned char> tc_img = make_tc_image(pd, scale);
+  g.scale_host = scale;
   // Behler tables
   std::vector<std::vector<unsigned char>> bt;
   std::vector<double> bt_rc;
@@ -459,6 +548,8 @@ int build_device_tables() {
   blob_bytes = align(blob_bytes + shift2.size() * 4);
   size_t off_sc32 = blob_bytes;
   blob_bytes = align(blob_bytes + scale32.size() * 4);
+  size_t off_tc = blob_bytes;
+  blob_bytes = align(blob_bytes + tc_img.size());
   size_t off_beh = blob_bytes;
   std::vector<size_t> beh_off;
   for (auto& b : bt) {
@@ -476,6 +567,7 @@ int build_device_tables() {
   cudaMemcpy(base + off_sc32, scale32.data(), scale32.size() * 4, cudaMemcpyHostToDevice);
   for (size_t q = 0; q < bt.size(); ++q)
     cudaMemcpy(base + off_beh + beh_off[q], bt[q].data(), bt[q].size(), cudaMemcpyHostToDevice);
+  if (!tc_img.empty()) cudaMemcpy(base + off_tc, tc_img.data(), tc_img.size(), cudaMemcpyHostToDevice);
   if (cudaDeviceSynchronize() != cudaSuccess) return AENET_ERR_CUDA;
   pd.shift = (const double*)(base + off_shift);
   pd.scale = (const double*)(base + off_scale);
@@ -484,6 +576,7 @@ int build_device_tables() {
   pd.shift2 = (const float2*)(base + off_sh2);
   pd.scale32 = (const float*)(base + off_sc32);
   pd.behler_blob = (const unsigned char*)(base + off_beh);
+  pd.tc_img = tc_img.empty() ? nullptr : (const unsigned char*)(base + off_tc);
   for (size_t q = 0; q < bt.size(); ++q) pd.sp[q].behler_off = (int)beh_off[q];
   g.pd = pd;
   g.blob = std::move(blob);
@@ -693,11 +786,11 @@ struct aenet_gpu_plan {
   double* E_struct = nullptr;
   double* virial = nullptr;
   unsigned* status = nullptr;
-  // training workspace, allocated by the first loss/gradient call
-  void* tmem = nullptr;
-  int* order = nullptr;       // atoms grouped by species
+  int* order = nullptr;       // atoms grouped by species (tensor-core networks, training)
   int* spec_off = nullptr;    // [AE_MAXT + 1]
   int* part_scratch = nullptr;
+  // training workspace, allocated by the first loss/gradient call
+  void* tmem = nullptr;
   double* cE = nullptr;       // [nstruc] dL/dE coefficients
   double* loss_s = nullptr;   // [nstruc]
   void* U = nullptr;          // [N] T4 dL/dF
@@ -915,6 +1008,9 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_Es = take(8 * (size_t)P->nstruc);
   size_t o_V = take(72 * (size_t)P->nstruc);
   size_t o_st = take(16);
+  size_t o_ord = take(4 * (size_t)N);
+  size_t o_spo = take(4 * (AE_MAXT + 1));
+  size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(N));
   if (cudaMalloc(&P->mem, off) != cudaSuccess) return AENET_ERR_CUDA;
   P->mem_bytes = off;
   char* b = (char*)P->mem;
@@ -942,6 +1038,9 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->E_struct = (double*)(b + o_Es);
   P->virial = (double*)(b + o_V);
   P->status = (unsigned*)(b + o_st);
+  P->order = (int*)(b + o_ord);
+  P->spec_off = (int*)(b + o_spo);
+  P->part_scratch = (int*)(b + o_ps);
   std::vector<int> as(N);
   for (int s = 0, a = 0; s < P->nstruc; ++s)
     for (int q = 0; q < P->natoms_h[s]; ++q) as[a++] = s;
@@ -1043,6 +1142,19 @@ int plan_forward(aenet_gpu_plan* P, const double* d_coords, const int* d_types, 
   return plan_eval(P, d_E, d_E_atoms, s);
 }
 
+// networks: tensor-core kernel on the mixed path when the networks fit it
+// (atoms grouped by species first), the SIMT kernel otherwise
+int plan_networks(aenet_gpu_plan* P, const DescBuffers& d, cudaStream_t s) {
+  const PotDevice& pd = *P->pd;
+  if (!P->fp64 && pd.tc_ok && g.networks_tc) {
+    if (ck(ae_launch_partition(P->natoms, pd.ntypes, P->types0, P->part_scratch, P->order,
+                               P->spec_off, s)))
+      return AENET_ERR_CUDA;
+    return ck(ae_launch_mlp_tc(pd, d, P->order, P->spec_off, s));
+  }
+  return ck(ae_launch_mlp(pd, d, P->fp64, s));
+}
+
 // descriptors + networks + energies on the current neighbour table
 int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s) {
   const PotDevice& pd = *P->pd;
@@ -1050,7 +1162,7 @@ int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s)
   int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
                                              : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
   if (ck(e)) return AENET_ERR_CUDA;
-  if (ck(ae_launch_mlp(pd, d, P->fp64, s))) return AENET_ERR_CUDA;
+  if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
   if (ck(ae_launch_energy_reduce(P->nstruc, P->geom_d, P->E_atom, P->E_struct, s))) return AENET_ERR_CUDA;
   if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
     return AENET_ERR_CUDA;
@@ -1695,6 +1807,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     g.cell_div = d;
     return AENET_OK;
   }
+  if (k == "networks") {
+    if (v == "tensor") g.networks_tc = 1;
+    else if (v == "simt") g.networks_tc = 0;
+    else return AENET_ERR_INPUT;
+    return AENET_OK;
+  }
   return AENET_ERR_INPUT;
 }
 
@@ -1779,9 +1897,6 @@ int plan_train_alloc(aenet_gpu_plan* P) {
     off = (off + bytes + 255) & ~(size_t)255;
     return o;
   };
-  size_t o_ord = take(4 * N);
-  size_t o_so = take(4 * (AE_MAXT + 1));
-  size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(P->natoms));
   size_t o_ce = take(8 * (size_t)P->nstruc);
   size_t o_ls = take(8 * (size_t)P->nstruc);
   size_t o_u = take(4 * tsz * N);
@@ -1791,9 +1906,6 @@ int plan_train_alloc(aenet_gpu_plan* P) {
     return AENET_ERR_CUDA;
   }
   char* b = (char*)P->tmem;
-  P->order = (int*)(b + o_ord);
-  P->spec_off = (int*)(b + o_so);
-  P->part_scratch = (int*)(b + o_ps);
   P->cE = (double*)(b + o_ce);
   P->loss_s = (double*)(b + o_ls);
   P->U = (void*)(b + o_u);
@@ -1896,6 +2008,7 @@ int md_build(aenet_gpu_md* M) {
     if (cudaMemcpyAsync(&h, P->status, 4, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
       return AENET_ERR_CUDA;
     if (h & (AE_ST_BAD_COORD | AE_ST_BAD_TYPE | AE_ST_CELL_OVERFLOW)) return AENET_ERR_INPUT;
+    if (h & AE_ST_TC_TIMEOUT) return AENET_ERR_CUDA;
     if (h & AE_ST_NB_OVERFLOW) {
       st = md_plan(M, ((M->cap * 3 / 2) + 31) & ~31);
       if (st) return st;
@@ -2129,6 +2242,13 @@ EXPORT int aenet_gpu_set_weights(const double* W) {
     if (cudaMemcpy(const_cast<double*>(g.pd.w64), w64.data(), 8 * w64.size(), cudaMemcpyHostToDevice) ||
         cudaMemcpy(const_cast<float*>(g.pd.w32), w32.data(), 4 * w32.size(), cudaMemcpyHostToDevice))
       return AENET_ERR_CUDA;
+    if (g.pd.tc_ok && g.pd.tc_img) {
+      PotDevice tmp = g.pd;
+      std::vector<unsigned char> img = make_tc_image(tmp, g.scale_host);
+      if (img.empty() || cudaMemcpy(const_cast<unsigned char*>(g.pd.tc_img), img.data(), img.size(),
+                                    cudaMemcpyHostToDevice))
+        return AENET_ERR_CUDA;
+    }
   }
   return AENET_OK;
 }
@@ -2167,7 +2287,7 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   e |= (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
                                           : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
   cudaEventRecord(ev[3], s);
-  e |= ae_launch_mlp(pd, d, P->fp64, s);
+  e |= plan_networks(P, d, s);
   cudaEventRecord(ev[4], s);
   e |= ae_launch_energy_reduce(P->nstruc, P->geom_d, P->E_atom, P->E_struct, s);
   if (d_E) cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s);
@@ -2319,6 +2439,10 @@ int batch_host(int nstruc, const int* natoms, const double* coords, const int* t
     }
     if (status & (AE_ST_BAD_COORD)) return AENET_ERR_INPUT;
     if (status & AE_ST_BAD_TYPE) return AENET_ERR_TYPE;
+    if (status & AE_ST_TC_TIMEOUT) {
+      c.reset();
+      return AENET_ERR_CUDA;
+    }
     if (status & (AE_ST_NB_OVERFLOW | AE_ST_CELL_OVERFLOW)) {
       // retry with larger capacities (the angular capacity follows cap)
       cap = P->cap * 2;

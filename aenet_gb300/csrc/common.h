@@ -33,6 +33,7 @@
 #define AE_ST_BAD_COORD 2u
 #define AE_ST_BAD_TYPE 4u
 #define AE_ST_CELL_OVERFLOW 8u
+#define AE_ST_TC_TIMEOUT 16u     // a tensor-core wait ran out of iterations
 
 enum { AE_SF_CHEBYSHEV = 1, AE_SF_BEHLER = 2 };
 
@@ -104,7 +105,46 @@ struct PotDevice {
   const double* w64;                  // weights, row-major W[o][k], pitch
   const float* w32;
   const unsigned char* behler_blob;   // BehlerTable per species
+  // tensor-core networks of the mixed path (two hidden layers): per species
+  // an image of split-BF16 operand tiles and FP32 vectors (TcLayout)
+  int tc_ok;                          // every species fits the tensor-core kernel
+  int tc_kin, tc_h;                   // padded input and hidden widths (32 or 64)
+  const unsigned char* tc_img;        // [ntypes][TcLayout::bytes]
 };
+
+// Per-species image for the tensor-core networks.  Operand tiles are
+// K-major in the canonical no-swizzle layout of the MMA shared-memory
+// descriptor: 8 x 8 (rows x BF16) core matrices of 128 contiguous bytes,
+// core matrices along K adjacent (leading byte offset 128), row blocks
+// (K/8) * 128 bytes apart (stride byte offset).  Each operand is stored as
+// a high part and a low part (x = hi + lo, both BF16), hi first.
+//   B1  [h][kin]   layer-1 weights W1[o][k]
+//   B2  [h][h]     layer-2 weights W2[o][k]
+//   B2T [h][h]     W2 transposed (rows k, columns o) for the backward pass
+//   B1T [kin][h]   W1 transposed
+//   vec (FP32)     b1[h] b2[h] w3[h] nsc[kin] {b3, f_a1, f_a2, f_a3}
+// Padded rows and columns are zero.
+struct TcLayout {
+  int kin, h;
+  int b1, b2, b2t, b1t, vec, bytes;
+};
+__host__ __device__ inline TcLayout tc_layout(int kin, int h) {
+  TcLayout L;
+  L.kin = kin;
+  L.h = h;
+  L.b1 = 0;
+  L.b2 = L.b1 + 4 * h * kin;
+  L.b2t = L.b2 + 4 * h * h;
+  L.b1t = L.b2t + 4 * h * h;
+  L.vec = L.b1t + 4 * kin * h;
+  L.bytes = L.vec + 4 * (3 * h + kin + 4);
+  L.bytes = (L.bytes + 127) & ~127;
+  return L;
+}
+// byte offset of element (r, k) of a K-major operand with K columns
+__host__ __device__ inline int tc_core_offset(int r, int k, int K) {
+  return ((r >> 3) * (K >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
 
 // ----------------------------------------------------------------------
 // Structures of a batch
@@ -191,6 +231,9 @@ int ae_launch_behler_adjoint(const PotDevice& pd, const DescBuffers& b,
                              int fp64, cudaStream_t s);
 int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64,
                   cudaStream_t s);
+// tensor-core networks (mixed path); atoms grouped by species in `order`
+int ae_launch_mlp_tc(const PotDevice& pd, const DescBuffers& b, const int* order,
+                     const int* spec_off, cudaStream_t s);
 int ae_fma_peak(double* tflops, cudaStream_t s);
 int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes,
                     unsigned* status, cudaStream_t s);

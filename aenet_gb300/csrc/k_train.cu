@@ -48,20 +48,38 @@ __global__ void k_part_count(int n, const int* __restrict__ types, int* __restri
   if (threadIdx.x < AE_MAXT) bcnt[blockIdx.x * AE_MAXT + threadIdx.x] = c[threadIdx.x];
 }
 
-// species-major exclusive scan of the block counts (one thread: a few
-// thousand additions)
+// species-major exclusive scan of the block counts: warp t scans the
+// column of species t; the species totals are prefixed first
 __global__ void k_part_scan(int nblk, int ntypes, const int* __restrict__ bcnt, int* __restrict__ boff,
                             int* __restrict__ spec_off) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int run = 0;
-  for (int t = 0; t < ntypes; ++t) {
-    spec_off[t] = run;
-    for (int b = 0; b < nblk; ++b) {
-      boff[b * AE_MAXT + t] = run;
-      run += bcnt[b * AE_MAXT + t];
+  __shared__ int tot[AE_MAXT];
+  const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+  if (t < ntypes) {
+    int s = 0;
+    for (int b = lane; b < nblk; b += 32) s += bcnt[b * AE_MAXT + t];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+    if (lane == 0) tot[t] = s;
+  }
+  __syncthreads();
+  if (t < ntypes) {
+    int run = 0;
+    for (int u = 0; u < t; ++u) run += tot[u];
+    if (lane == 0) spec_off[t] = run;
+    if (t == ntypes - 1 && lane == 0) spec_off[ntypes] = run + tot[t];
+    for (int b0 = 0; b0 < nblk; b0 += 32) {
+      const int b = b0 + lane;
+      const int c = b < nblk ? bcnt[b * AE_MAXT + t] : 0;
+      int x = c;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+      }
+      if (b < nblk) boff[b * AE_MAXT + t] = run + x - c;
+      run += __shfl_sync(0xffffffffu, x, 31);
     }
   }
-  spec_off[ntypes] = run;
 }
 
 __global__ void k_part_scatter(int n, int ntypes, const int* __restrict__ types,
@@ -475,7 +493,7 @@ int ae_launch_partition(int natoms, int ntypes, const int* types0, int* scratch,
   int* bcnt = scratch;
   int* boff = scratch + AE_MAXT * nblk;
   k_part_count<<<nblk, PART_B, 0, s>>>(natoms, types0, bcnt);
-  k_part_scan<<<1, 32, 0, s>>>(nblk, ntypes, bcnt, boff, spec_off);
+  k_part_scan<<<1, 32 * AE_MAXT, 0, s>>>(nblk, ntypes, bcnt, boff, spec_off);
   k_part_scatter<<<nblk, PART_B, 0, s>>>(natoms, ntypes, types0, boff, order);
   return (int)cudaGetLastError();
 }

@@ -25,6 +25,7 @@ ST_NB_OVERFLOW = 1
 ST_BAD_COORD = 2
 ST_BAD_TYPE = 4
 ST_CELL_OVERFLOW = 8
+ST_TC_TIMEOUT = 16
 
 
 class PlanStatusError(RuntimeError):
@@ -199,7 +200,8 @@ class Plan:
             names = [n for b, n in ((ST_NB_OVERFLOW, "neighbour capacity overflow"),
                                     (ST_BAD_COORD, "non-finite coordinate"),
                                     (ST_BAD_TYPE, "invalid type id"),
-                                    (ST_CELL_OVERFLOW, "cell capacity overflow")) if st & b]
+                                    (ST_CELL_OVERFLOW, "cell capacity overflow"),
+                                    (ST_TC_TIMEOUT, "tensor-core wait timed out")) if st & b]
             raise PlanStatusError("plan status %d: %s" % (st, ", ".join(names)))
 
     def neighbors(self):

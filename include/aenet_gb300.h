@@ -41,6 +41,11 @@ extern "C" {
  *                potentials shipped with aenet were trained with.
  *   "cell_div" = "1" | "2" | "3"   cells per cut-off length in the
  *       neighbour search grid (performance only).
+ *   "lanes_per_atom" = "8" | "16" | "32"   descriptor kernels' lanes per
+ *       atom (performance only).
+ *   "networks" = "tensor" | "simt"   mixed-path networks on the tcgen05
+ *       tensor cores (split BF16, FP32 accumulation; networks with two
+ *       hidden layers and widths up to 64) or on FP32 SIMT.
  * Returns AENET_OK or AENET_ERR_INPUT.  Takes effect at the next load or
  * plan creation. */
 int aenet_gpu_set_option(const char* key, const char* value);
@@ -124,6 +129,7 @@ int aenet_gpu_measure_fp32_peak(double* tflops, void* stream);
 #define AENET_GPU_ST_BAD_COORD 2u
 #define AENET_GPU_ST_BAD_TYPE 4u
 #define AENET_GPU_ST_CELL_OVERFLOW 8u
+#define AENET_GPU_ST_TC_TIMEOUT 16u   /* a tensor-core wait gave up (results invalid) */
 unsigned aenet_gpu_plan_status(aenet_gpu_plan* plan, void* stream);
 
 /* Neighbour table of the last run (device pointers, for inspection and

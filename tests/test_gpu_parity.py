@@ -440,3 +440,39 @@ def test_rutile_behler_fp64_parity_virial_and_mixed(cuda, oracle, rutile):
     assert abs(r32["energy"] - r64["energy"]) / n < E_TOL_MIXED
     dF = r32["forces"] - r64["forces"]
     assert np.sqrt(np.mean(dF ** 2)) < F_RMS_MIXED
+
+
+@pytest.mark.parametrize("which", ["lisio", "aucu"])
+def test_tensor_core_networks_match_simt_and_fp64(cuda, oracle, aucu, tmp_path, which):
+    """tcgen05 networks (split BF16, FP32 accumulation in TMEM) against the
+    SIMT FP32 kernel and the FP64 path: 32-32-32-1 x3 (kin 32) and
+    40-25-25-1 x2 (kin 64, hidden padded to 32)."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    if which == "lisio":
+        w = workloads.lisio_batch_4096(nstruc=24)
+        paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    else:
+        w, paths = aucu
+    ann = _ann(paths, w.types)
+    try:
+        structs = [(s.positions, s.types, s.cell, True) for s in w.structures]
+        r64 = ann.batch_energy_forces(structs, precision=FP64)
+        out = {}
+        for mode in ("simt", "tensor"):
+            set_option("networks", mode)
+            out[mode] = ann.batch_energy_forces(structs, precision=MIXED)
+    finally:
+        set_option("networks", "tensor")
+        ann.release()
+    nat = np.array([s.natoms for s in w.structures])
+    for mode in ("simt", "tensor"):
+        dE = np.abs(out[mode]["energy"] - r64["energy"]) / nat
+        dF = out[mode]["forces"] - r64["forces"]
+        assert dE.max() < E_TOL_MIXED, (mode, dE.max())
+        assert np.sqrt((dF ** 2).mean()) < F_RMS_MIXED, mode
+    # split BF16 keeps ~16 bits: far inside the mixed tolerance
+    dE = np.abs(out["tensor"]["energy"] - out["simt"]["energy"]) / nat
+    assert dE.max() < 1e-4
+    dF = out["tensor"]["forces"] - out["simt"]["forces"]
+    assert np.sqrt((dF ** 2).mean()) < 1e-3
