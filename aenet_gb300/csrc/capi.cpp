@@ -374,6 +374,7 @@ int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<doubl
 std::vector<unsigned char> make_tc_image(PotDevice& pd, const std::vector<double>& scale) {
   std::vector<unsigned char> tc_img;
   pd.tc_ok = 0;
+  pd.tc_tanh = 0;
   {
     bool ok = true;
     int kin = 0, h = 0;
@@ -431,6 +432,11 @@ std::vector<unsigned char> make_tc_image(PotDevice& pd, const std::vector<double
       pd.tc_ok = 1;
       pd.tc_kin = kin;
       pd.tc_h = h;
+      pd.tc_tanh = 1;
+      for (int t = 0; t < g.ntypes; ++t) {
+        const HostNet& net = g.pots[t].net;
+        if (net.f_a[0] != 1 || net.f_a[1] != 1 || net.f_a[2] != 0) pd.tc_tanh = 0;
+      }
     }
   }
   return tc_img;

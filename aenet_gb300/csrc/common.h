@@ -109,6 +109,7 @@ struct PotDevice {
   // an image of split-BF16 operand tiles and FP32 vectors (TcLayout)
   int tc_ok;                          // every species fits the tensor-core kernel
   int tc_kin, tc_h;                   // padded input and hidden widths (32 or 64)
+  int tc_tanh;                        // every species: tanh hidden layers, linear output
   const unsigned char* tc_img;        // [ntypes][TcLayout::bytes]
 };
 

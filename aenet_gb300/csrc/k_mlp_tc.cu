@@ -91,19 +91,23 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane
+// 32 consecutive FP32 columns of this thread's TMEM lane.  The load and
+// its wait are one asm statement: the destination registers are written
+// asynchronously, so no instruction may read them before the wait, and
+// the compiler only orders uses after the statement that defines them.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   uint32_t r[32];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%"
-      "15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      "tcgen05.wait::ld.sync.aligned;"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
         "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
         "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
         "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
   for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
@@ -169,7 +173,34 @@ __device__ __forceinline__ void activate(int t, float x, float& y, float& dy) {
   }
 }
 
-template <int KIN, int H>
+// tanh(x) = 1 - 2 / (exp(2x) + 1): absolute error ~1e-7, far below the
+// ~1e-5 relative resolution of the split-BF16 operands it feeds
+__device__ __forceinline__ float tanh_fast(float x) {
+  return 1.f - __fdividef(2.f, __expf(2.f * x) + 1.f);
+}
+
+// activation of a whole row: a = f(z + bias), d = f'(z + bias)
+template <int N, bool TANH>
+__device__ __forceinline__ void act_row(int fa, float* z, const float* bias, float* d) {
+  if (TANH) {
+#pragma unroll
+    for (int n = 0; n < N; ++n) {
+      const float y = tanh_fast(z[n] + bias[n]);
+      z[n] = y;
+      d[n] = 1.f - y * y;
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < N; ++n) {
+      float y, dy;
+      activate(fa, z[n] + bias[n], y, dy);
+      z[n] = y;
+      d[n] = dy;
+    }
+  }
+}
+
+template <int KIN, int H, bool TANH>
 __global__ void __launch_bounds__(128) k_mlp_tc(PotDevice pd, DescBuffers b,
                                                 const int* __restrict__ order,
                                                 const int* __restrict__ spec_off, int tiles_ub) {
@@ -228,6 +259,7 @@ __global__ void __launch_bounds__(128) k_mlp_tc(PotDevice pd, DescBuffers b,
       uint4* dst = reinterpret_cast<uint4*>(img);
       for (int k = m; k < L.bytes / 16; k += TILE) dst[k] = src[k];
       cur = t;
+      __syncthreads();   // every thread reads parts of the image the others copied
     }
     const float* vec = reinterpret_cast<const float*>(img + L.vec);
     const float* b1 = vec;
@@ -272,13 +304,7 @@ __global__ void __launch_bounds__(128) k_mlp_tc(PotDevice pd, DescBuffers b,
     {
       float z[H];
       tmem_ld<H>(tlane, z);
-#pragma unroll
-      for (int n = 0; n < H; ++n) {
-        float a, d;
-        activate(fa1, z[n] + b1[n], a, d);
-        z[n] = a;
-        f1p[n] = d;
-      }
+      act_row<H, TANH>(fa1, z, b1, f1p);
       store_split<H / 8>(bHi, bLo, m, z);
     }
     fence_proxy_async();
@@ -297,16 +323,17 @@ __global__ void __launch_bounds__(128) k_mlp_tc(PotDevice pd, DescBuffers b,
     {
       float z[H];
       tmem_ld<H>(tlane, z);
+      float d2[H];
+      act_row<H, TANH>(fa2, z, b2, d2);
       float s = b3;
 #pragma unroll
       for (int n = 0; n < H; ++n) {
-        float a, d;
-        activate(fa2, z[n] + b2[n], a, d);
-        s = fmaf(w3[n], a, s);
-        z[n] = w3[n] * d;
+        s = fmaf(w3[n], z[n], s);
+        z[n] = w3[n] * d2[n];
       }
-      float dy;
-      activate(fa3, s, y, dy);
+      float dy = 1.f;
+      y = s;
+      if (!TANH) activate(fa3, s, y, dy);
 #pragma unroll
       for (int n = 0; n < H; ++n) z[n] *= dy;
       store_split<H / 8>(aHi, aLo, m, z);
@@ -382,16 +409,18 @@ size_t tc_smem() {
   return (size_t)tc_layout(KIN, H).bytes + 2 * TILE * KA * 2 + 2 * TILE * H * 2 + 16;
 }
 
-template <int KIN, int H>
+template <int KIN, int H, bool TANH>
 int launch_tc(const PotDevice& pd, const DescBuffers& b, const int* order, const int* spec_off,
               cudaStream_t s) {
   const size_t smem = tc_smem<KIN, H>();
-  auto kern = k_mlp_tc<KIN, H>;
+  auto kern = k_mlp_tc<KIN, H, TANH>;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int dev = 0, nsm = 148, occ = 1;
+  int dev = 0, nsm = 148, smem_sm = 228 * 1024;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TILE, smem);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  // CTAs per SM by shared memory (1 KB reserved per CTA) and TMEM columns
+  int occ = (int)(smem_sm / (smem + 1024));
   occ = max(1, min(occ, (int)(512 / TMEM_COLS)));
   const int tiles_ub = (b.natoms + TILE - 1) / TILE + pd.ntypes;
   const int grid = max(1, min(tiles_ub, nsm * occ));
@@ -405,9 +434,15 @@ int ae_launch_mlp_tc(const PotDevice& pd, const DescBuffers& b, const int* order
                      const int* spec_off, cudaStream_t s) {
   if (b.natoms <= 0) return 0;
   if (!pd.tc_ok || !pd.tc_img) return (int)cudaErrorInvalidValue;
-  if (pd.tc_kin == 32 && pd.tc_h == 32) return launch_tc<32, 32>(pd, b, order, spec_off, s);
-  if (pd.tc_kin == 64 && pd.tc_h == 32) return launch_tc<64, 32>(pd, b, order, spec_off, s);
-  if (pd.tc_kin == 32 && pd.tc_h == 64) return launch_tc<32, 64>(pd, b, order, spec_off, s);
-  if (pd.tc_kin == 64 && pd.tc_h == 64) return launch_tc<64, 64>(pd, b, order, spec_off, s);
+  if (pd.tc_tanh) {
+    if (pd.tc_kin == 32 && pd.tc_h == 32) return launch_tc<32, 32, true>(pd, b, order, spec_off, s);
+    if (pd.tc_kin == 64 && pd.tc_h == 32) return launch_tc<64, 32, true>(pd, b, order, spec_off, s);
+    if (pd.tc_kin == 32 && pd.tc_h == 64) return launch_tc<32, 64, true>(pd, b, order, spec_off, s);
+    if (pd.tc_kin == 64 && pd.tc_h == 64) return launch_tc<64, 64, true>(pd, b, order, spec_off, s);
+  }
+  if (pd.tc_kin == 32 && pd.tc_h == 32) return launch_tc<32, 32, false>(pd, b, order, spec_off, s);
+  if (pd.tc_kin == 64 && pd.tc_h == 32) return launch_tc<64, 32, false>(pd, b, order, spec_off, s);
+  if (pd.tc_kin == 32 && pd.tc_h == 64) return launch_tc<32, 64, false>(pd, b, order, spec_off, s);
+  if (pd.tc_kin == 64 && pd.tc_h == 64) return launch_tc<64, 64, false>(pd, b, order, spec_off, s);
   return (int)cudaErrorInvalidValue;
 }
