@@ -1,11 +1,14 @@
 """Measured choice of the evaluator's launch shapes.
 
-Two knobs decide most of the run time of a batch: the number of lanes that
-cooperate on one atom in the descriptor and adjoint kernels (8, 16 or 32)
-and the number of neighbour-search cells per cut-off length (1, 2 or 3).
-:func:`tune` times a full energy-and-force pass of the caller's batch for
-every combination (CUDA events on the current stream) and keeps the
-fastest; results are cached per workload key in a JSON file.
+Three knobs decide most of the run time of a batch: the neighbour-search
+kernel (one warp per home cell or per atom), the number of neighbour-search
+cells per cut-off length (1, 2 or 3) and the number of lanes that cooperate
+on one atom in the descriptor and adjoint kernels (8, 16 or 32).  The first
+two only change the neighbour search and the last only the descriptor
+kernels, so :func:`tune` times a full energy-and-force pass of the caller's
+batch (CUDA events on the current stream) over the search settings at a
+fixed lane count, then over the lane counts at the best search setting;
+results are cached per workload key in a JSON file.
 """
 import json
 import os
@@ -17,6 +20,7 @@ from .plan import Plan
 
 LANES = (8, 16, 32)
 CELL_DIVS = (1, 2, 3)
+NB_KERNELS = ("cell", "atom")
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "aenet_gb300", "autotune.json")
 
 
@@ -37,8 +41,9 @@ def _time(plan, p, t, reps):
 
 
 def tune(natoms, cells, pbc, positions, types, precision=core.MIXED, key=None, reps=3,
-         cache=CACHE, lanes=LANES, cell_divs=CELL_DIVS):
-    """Return (lanes_per_atom, cell_div, ms) and apply them as options."""
+         cache=CACHE, lanes=LANES, cell_divs=CELL_DIVS, nb_kernels=NB_KERNELS):
+    """Return the chosen {neighbour_kernel, cell_div, lanes_per_atom, ms}
+    and apply them as options."""
     entries = {}
     if key and cache and os.path.exists(cache):
         try:
@@ -51,16 +56,26 @@ def tune(natoms, cells, pbc, positions, types, precision=core.MIXED, key=None, r
         p = torch.as_tensor(positions, dtype=torch.float64, device="cuda").contiguous()
         t = torch.as_tensor(types, dtype=torch.int32, device="cuda").contiguous()
         results = []
+        lp0 = lanes[0]
+        core.set_option("lanes_per_atom", lp0)
         for cd in cell_divs:
             core.set_option("cell_div", cd)
             plan = Plan(natoms, cells, pbc, precision=precision, coords0=positions)
-            for lp in lanes:
-                core.set_option("lanes_per_atom", lp)
-                results.append((_time(plan, p, t, reps), lp, cd))
+            for nk in nb_kernels:
+                core.set_option("neighbour_kernel", nk)
+                results.append((_time(plan, p, t, reps), lp0, cd, nk))
             plan.close()
-        ms, lp, cd = min(results)
-        best = {"lanes_per_atom": lp, "cell_div": cd, "ms": ms,
-                "all": [[r[1], r[2], r[0]] for r in results]}
+        _, _, cd, nk = min(results)
+        core.set_option("cell_div", cd)
+        core.set_option("neighbour_kernel", nk)
+        plan = Plan(natoms, cells, pbc, precision=precision, coords0=positions)
+        for lp in lanes[1:]:
+            core.set_option("lanes_per_atom", lp)
+            results.append((_time(plan, p, t, reps), lp, cd, nk))
+        plan.close()
+        ms, lp, cd, nk = min(results)
+        best = {"neighbour_kernel": nk, "cell_div": cd, "lanes_per_atom": lp, "ms": ms,
+                "all": [[r[3], r[2], r[1], r[0]] for r in results]}
         if key and cache:
             os.makedirs(os.path.dirname(cache), exist_ok=True)
             entries[key] = best
@@ -69,4 +84,5 @@ def tune(natoms, cells, pbc, positions, types, precision=core.MIXED, key=None, r
             os.replace(tmp, cache)
     core.set_option("lanes_per_atom", best["lanes_per_atom"])
     core.set_option("cell_div", best["cell_div"])
+    core.set_option("neighbour_kernel", best.get("neighbour_kernel", "cell"))
     return best

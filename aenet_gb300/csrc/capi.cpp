@@ -268,6 +268,7 @@ struct State {
   int cell_div = 2;
   int lpa_default = 16;
   int networks_tc = 1;       // tensor-core networks on the mixed path when eligible
+  int nb_cell = 0;           // neighbour search: one warp per home cell (1) or per atom (0)
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
@@ -1131,6 +1132,7 @@ NbBuffers nb_buffers(aenet_gpu_plan* P) {
   nb.nb_vec = P->nb_vec;
   nb.nb_img = P->nb_img;
   nb.status = P->status;
+  nb.cell_kernel = g.nb_cell;
   return nb;
 }
 
@@ -1811,6 +1813,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     int d = atoi(v.c_str());
     if (d < 1 || d > 3) return AENET_ERR_INPUT;
     g.cell_div = d;
+    return AENET_OK;
+  }
+  if (k == "neighbour_kernel") {
+    if (v == "cell") g.nb_cell = 1;
+    else if (v == "atom") g.nb_cell = 0;
+    else return AENET_ERR_INPUT;
     return AENET_OK;
   }
   if (k == "networks") {

@@ -194,6 +194,7 @@ struct NbBuffers {
   void* nb_vec;               // float4 or double4_32a
   int* nb_img;                // optional: image T packed 3 x 10-bit signed
   unsigned* status;
+  int cell_kernel;            // 1: one warp per home cell, 0: one warp per atom
 };
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types,

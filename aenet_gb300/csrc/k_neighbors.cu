@@ -178,6 +178,8 @@ __global__ void k_scatter(int natoms, NbBuffers nb) {
   nb.cell_pos[p] = nb.r_f32[i];
 }
 
+__device__ __forceinline__ int sext10i(int v) { return (v ^ 512) - 512; }
+
 __device__ __forceinline__ int floor_div(int a, int n) {
   int q = a / n;
   return (a % n != 0 && (a < 0)) ? q - 1 : q;
@@ -393,6 +395,225 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
   }
 }
 
+// ---- cell-batched search: one warp per home cell, lane h = home atom h.
+// Candidates (the same stencil units as above, pruned for the whole home
+// cell in orthogonal cells) are staged 32 at a time in shared memory and
+// every lane tests each of them against its own home atom, appending
+// accepted pairs to its own row: no ballots or shuffles in the inner loop,
+// and the unit mapping and candidate loads are shared by the cell's atoms.
+// Acceptance is the same FP32 filter + FP64 band test.
+constexpr int NBC_WARPS = 8;
+
+template <typename T4>
+__global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb) {
+  __shared__ float4 s_pos[NBC_WARPS][32];     // candidate position, species bits in w
+  __shared__ float4 s_shift[NBC_WARPS][32];   // image shift, packed image in w
+  __shared__ int s_j[NBC_WARPS][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gc = blockIdx.x * NBC_WARPS + warp;
+  if (gc >= ncells) return;
+  const int hb = nb.cell_start[gc], he = nb.cell_start[gc + 1];
+  if (hb >= he) return;
+  int lo = 0, hi = nb.nstruc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (nb.geom[mid].cell_off <= gc) lo = mid; else hi = mid - 1;
+  }
+  const StructGeom* g = nb.geom + lo;
+  const int pbc = g->pbc;
+  const int nc0 = g->nc[0], nc1 = g->nc[1], nc2 = g->nc[2];
+  const int k0 = g->kr[0], k1 = g->kr[1], k2 = g->kr[2];
+  const int w1 = 2 * k1 + 1;
+  const int lin = gc - g->cell_off;
+  const int c2 = lin % nc2, c1 = (lin / nc2) % nc1, c0 = lin / (nc1 * nc2);
+  const int t2lo = pbc ? floor_div(c2 - k2, nc2) : 0;
+  const int t2hi = pbc ? floor_div(c2 + k2, nc2) : 0;
+  const int nt2 = t2hi - t2lo + 1;
+  const int nunits = (2 * k0 + 1) * w1 * nt2;
+  const float rc2_lo = g->rc2_lo, rc2_hi = g->rc2_hi;
+  const double rc2 = g->rc2;
+  const int cap = nb.cap;
+  const int* __restrict__ cstart = nb.cell_start + g->cell_off;
+  const float rcf = g->rcf * 1.0001f + 1e-4f;
+
+  for (int hbase = hb; hbase < he; hbase += 32) {
+    const bool home = hbase + lane < he;
+    const int ih = home ? nb.cell_atoms[hbase + lane] : -1;
+    const float4 rh = home ? nb.cell_pos[hbase + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const size_t row = (size_t)(home ? ih : 0) * cap;
+    int cnt = 0;
+    for (int ubase = 0; ubase < nunits; ubase += 32) {
+      const int u = ubase + lane;
+      int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
+      float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
+      if (u < nunits) {
+        const int it2 = u % nt2;
+        const int rr = u / nt2;
+        const int d1 = rr % w1 - k1;
+        const int d0 = rr / w1 - k0;
+        int a0 = c0 + d0, a1 = c1 + d1;
+        bool ok = true;
+        int zlo = c2 - k2, zhi = c2 + k2;
+        if (g->ortho) {
+          // gap between the home cell and row (a0, a1), whole cells apart
+          const float gx = (float)max(0, abs(d0) - 1) * g->hf[0] / nc0;
+          const float gy = (float)max(0, abs(d1) - 1) * g->hf[1] / nc1;
+          const float rem = rcf * rcf - gx * gx - gy * gy;
+          if (rem < 0.f) {
+            ok = false;
+          } else {
+            const int hz = 1 + (int)floorf(sqrtf(rem) / g->hf[2] * nc2 * 1.0001f + 1e-4f);
+            zlo = max(zlo, c2 - hz);
+            zhi = min(zhi, c2 + hz);
+          }
+        }
+        if (pbc) {
+          T0 = floor_div(a0, nc0);
+          a0 -= T0 * nc0;
+          T1 = floor_div(a1, nc1);
+          a1 -= T1 * nc1;
+          T2 = t2lo + it2;
+          zlo = max(zlo, T2 * nc2);
+          zhi = min(zhi, T2 * nc2 + nc2 - 1);
+        } else {
+          ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
+          zlo = max(zlo, 0);
+          zhi = min(zhi, nc2 - 1);
+        }
+        if (ok && zlo <= zhi) {
+          const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
+          beg = cstart[base + zlo];
+          len = cstart[base + zhi + 1] - beg;
+          const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
+          sh0 = f0 * g->Lf[0] + f1 * g->Lf[3] + f2 * g->Lf[6];
+          sh1 = f0 * g->Lf[1] + f1 * g->Lf[4] + f2 * g->Lf[7];
+          sh2 = f0 * g->Lf[2] + f1 * g->Lf[5] + f2 * g->Lf[8];
+        }
+      }
+      int incl = len;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int w = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += w;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      for (int qb = 0; qb < total; qb += 32) {
+        // ---- stage 32 candidates
+        const int q = qb + lane;
+        int lo2 = 0, hi2 = 31;
+#pragma unroll
+        for (int step = 0; step < 5; ++step) {
+          const int mid = (lo2 + hi2) >> 1;
+          const int pv = __shfl_sync(0xffffffffu, incl, mid);
+          if (pv > q) hi2 = mid; else lo2 = mid + 1;
+        }
+        const int own = lo2;
+        const int own_incl = __shfl_sync(0xffffffffu, incl, own);
+        const int own_len = __shfl_sync(0xffffffffu, len, own);
+        const int own_beg = __shfl_sync(0xffffffffu, beg, own);
+        const int oT0 = __shfl_sync(0xffffffffu, T0, own);
+        const int oT1 = __shfl_sync(0xffffffffu, T1, own);
+        const int oT2 = __shfl_sync(0xffffffffu, T2, own);
+        const float osh0 = __shfl_sync(0xffffffffu, sh0, own);
+        const float osh1 = __shfl_sync(0xffffffffu, sh1, own);
+        const float osh2 = __shfl_sync(0xffffffffu, sh2, own);
+        if (q < total) {
+          const int p = own_beg + (q - (own_incl - own_len));
+          s_pos[warp][lane] = nb.cell_pos[p];
+          s_j[warp][lane] = nb.cell_atoms[p];
+          s_shift[warp][lane] = make_float4(
+              osh0, osh1, osh2,
+              __int_as_float((oT0 & 1023) | ((oT1 & 1023) << 10) | ((oT2 & 1023) << 20)));
+        }
+        __syncwarp();
+        // ---- test them against this lane's home atom
+        const int nq = min(32, total - qb);
+        if (home) {
+          for (int c = 0; c < nq; ++c) {
+            const float4 rj = s_pos[warp][c];
+            const float4 sh = s_shift[warp][c];
+            const int j = s_j[warp][c];
+            const int img = __float_as_int(sh.w);
+            if (j == ih && img == 0) continue;   // the atom itself
+            const float dx = (rj.x - rh.x) + sh.x;
+            const float dy = (rj.y - rh.y) + sh.y;
+            const float dz = (rj.z - rh.z) + sh.z;
+            const float dd2 = dx * dx + dy * dy + dz * dz;
+            if (dd2 > rc2_hi) continue;
+            const int t0 = sext10i(img & 1023), t1 = sext10i((img >> 10) & 1023),
+                      t2 = sext10i((img >> 20) & 1023);
+            if (dd2 >= rc2_lo) {
+              // exact FP64 predicate, evaluated as the reference does
+              double e2;
+              if (pbc) {
+                double cart[3];
+                if (j == ih) {
+                  for (int cc = 0; cc < 3; ++cc) {
+                    double t = dm(g->L[cc], (double)t0);
+                    t = da(t, dm(g->L[3 + cc], (double)t1));
+                    t = da(t, dm(g->L[6 + cc], (double)t2));
+                    cart[cc] = t;
+                  }
+                } else {
+                  const double* sj = nb.s_wrap + 3 * j;
+                  const double u0 = da(sj[0], (double)t0), u1 = da(sj[1], (double)t1),
+                               u2 = da(sj[2], (double)t2);
+                  for (int cc = 0; cc < 3; ++cc) {
+                    double t = dm(g->L[cc], u0);
+                    t = da(t, dm(g->L[3 + cc], u1));
+                    t = da(t, dm(g->L[6 + cc], u2));
+                    cart[cc] = da(t, -nb.r_wrap[3 * ih + cc]);
+                  }
+                }
+                e2 = da(da(dm(cart[0], cart[0]), dm(cart[1], cart[1])), dm(cart[2], cart[2]));
+              } else {
+                const double c0d = da(nb.r_wrap[3 * j], -nb.r_wrap[3 * ih]);
+                const double c1d = da(nb.r_wrap[3 * j + 1], -nb.r_wrap[3 * ih + 1]);
+                const double c2d = da(nb.r_wrap[3 * j + 2], -nb.r_wrap[3 * ih + 2]);
+                e2 = da(da(dm(c0d, c0d), dm(c1d, c1d)), dm(c2d, c2d));
+              }
+              if (!(e2 <= rc2)) continue;
+            }
+            if (cnt < cap) {
+              nb.nb_jt[row + cnt] = j | (__float_as_int(rj.w) << AE_TYPE_SHIFT);
+              if (nb.nb_img) nb.nb_img[row + cnt] = img;
+              if (VecOut<T4>::fp64) {
+                double R[3];
+                if (pbc) {
+                  const double* sj = nb.s_wrap + 3 * j;
+                  const double u0 = da(sj[0], (double)t0), u1 = da(sj[1], (double)t1),
+                               u2 = da(sj[2], (double)t2);
+                  for (int cc = 0; cc < 3; ++cc) {
+                    double t = dm(g->L[cc], u0);
+                    t = da(t, dm(g->L[3 + cc], u1));
+                    t = da(t, dm(g->L[6 + cc], u2));
+                    R[cc] = da(t, -nb.r_wrap[3 * ih + cc]);
+                  }
+                } else {
+                  for (int cc = 0; cc < 3; ++cc)
+                    R[cc] = da(nb.r_wrap[3 * j + cc], -nb.r_wrap[3 * ih + cc]);
+                }
+                const double dist = sqrt(da(da(dm(R[0], R[0]), dm(R[1], R[1])), dm(R[2], R[2])));
+                reinterpret_cast<double4_32a*>(nb.nb_vec)[row + cnt] =
+                    make_double4_32a(R[0], R[1], R[2], dist);
+              } else {
+                reinterpret_cast<float4*>(nb.nb_vec)[row + cnt] =
+                    make_float4(dx, dy, dz, sqrtf(dd2));
+              }
+            }
+            ++cnt;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (home) {
+      nb.nb_cnt[ih] = min(cnt, cap);
+      if (cnt > cap) atomicOr(nb.status, AE_ST_NB_OVERFLOW);
+    }
+  }
+}
+
 }  // namespace
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types, const NbBuffers& nb,
@@ -408,6 +629,15 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
   k_scan_sums<<<1, SCAN_B, 0, s>>>(nblk, nb.scan_tmp, nb.cell_start + nc);
   k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
   k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
+  if (nb.cell_kernel) {
+    // zero counts first: empty home cells launch no work for their atoms
+    const int blocks = (nc + NBC_WARPS - 1) / NBC_WARPS;
+    if (fp64)
+      k_neighbors_cell<double4_32a><<<blocks, 32 * NBC_WARPS, 0, s>>>(nc, nb);
+    else
+      k_neighbors_cell<float4><<<blocks, 32 * NBC_WARPS, 0, s>>>(nc, nb);
+    return (int)cudaGetLastError();
+  }
   const int blocks = (natoms + 7) / 8;
   if (fp64)
     k_neighbors<double4_32a><<<blocks, 256, 0, s>>>(natoms, nb);

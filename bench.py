@@ -61,6 +61,8 @@ def parse():
                     help="fix the descriptor kernels' lanes per atom (implies --no-tune)")
     ap.add_argument("--cell-div", type=int, default=0,
                     help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
+    ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom"],
+                    help="fix the neighbour-search kernel (implies --no-tune)")
     ap.add_argument("--no-md", action="store_true", help="skip the 1M-atom MD leg")
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
@@ -274,14 +276,16 @@ def run_gb300(args):
     stream = torch.cuda.current_stream()
     tuned = None
     from aenet_gb300 import core as _core
-    if args.lanes_per_atom or args.cell_div:
+    if args.lanes_per_atom or args.cell_div or args.neighbour_kernel:
         args.no_tune = True
         if args.lanes_per_atom:
             _core.set_option("lanes_per_atom", args.lanes_per_atom)
         if args.cell_div:
             _core.set_option("cell_div", args.cell_div)
+        if args.neighbour_kernel:
+            _core.set_option("neighbour_kernel", args.neighbour_kernel)
         tuned = {"lanes_per_atom": args.lanes_per_atom or None, "cell_div": args.cell_div or None,
-                 "fixed": True}
+                 "neighbour_kernel": args.neighbour_kernel or None, "fixed": True}
     if not args.no_tune:
         from aenet_gb300 import autotune
         tuned = autotune.tune(nat, cells, pbc, pos, typ, precision=MIXED, cache=None)
@@ -355,7 +359,7 @@ def run_gb300(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
     kernels = {"descriptor": "k_cheb_forward", "adjoint": "k_cheb_adjoint",
-               "networks": "k_mlp", "neighbours": "k_neighbors"}
+               "networks": "k_mlp_tc", "neighbours": "k_neighbors"}
     dom = max(kernels, key=lambda k: stages.get(k, 0.0))
     cap = nb["cap"]
     # algorithmic bytes per atom of each kernel (neighbour table at 20 B per
@@ -505,8 +509,9 @@ def run_gb300(args):
     else:
         ann.release()
 
-    launches_per_step = 12   # types, 6 neighbour-search kernels, descriptor, networks,
-    #                          energy reduction, adjoint, force output
+    launches_per_step = 15   # types, 6 neighbour-search kernels, descriptor, 3 species-
+    #                          partition kernels, tensor-core networks, energy reduction,
+    #                          adjoint, force output
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,

@@ -49,6 +49,16 @@ def aucu(oracle, tmp_path_factory):
     return w, paths
 
 
+@pytest.fixture(params=["atom", "cell"])
+def nb_kernel(request, cuda):
+    """Run a test with either neighbour-search kernel (one warp per atom or
+    one warp per home cell); restores the default afterwards."""
+    from aenet_gb300.core import set_option
+    set_option("neighbour_kernel", request.param)
+    yield request.param
+    set_option("neighbour_kernel", "atom")
+
+
 def _ann(paths, types, angular=None):
     from aenet_gb300.core import ANNPotentials
     return ANNPotentials({t: paths[t] for t in types}, angular_domain=angular or "current")
@@ -118,7 +128,7 @@ def test_cu256_virial_matches_strain_derivative(cuda, oracle, cu256):
     assert np.abs(r["virial"] - W).max() < 1e-5 * max(1.0, np.abs(W).max())
 
 
-def test_neighbour_sets_bit_exact(cuda, oracle, cu256):
+def test_neighbour_sets_bit_exact(cuda, oracle, cu256, nb_kernel):
     """aenet_nbl_* against the oracle's complete lcl_nbdist_cart lists on the
     same lattice coordinates: identical (atom, image) sets and coordinates."""
     from aenet_gb300 import _lib, workloads
@@ -268,7 +278,7 @@ def test_autograd_adjoint_and_finite_differences(cuda, aucu):
         ann.release()
 
 
-def test_batch_of_small_cells_matches_oracle(cuda, oracle, tmp_path):
+def test_batch_of_small_cells_matches_oracle(cuda, oracle, tmp_path, nb_kernel):
     """Several small periodic cells (cut-off longer than the cell: many
     images) in one batched call, FP64 against the oracle per structure."""
     from aenet_gb300 import workloads
@@ -349,7 +359,7 @@ def test_capacity_overflow_is_reported_and_retried(cuda, cu256):
         ann.release()
 
 
-def test_fp32_and_fp64_plans_find_the_same_neighbours(cuda, oracle, tmp_path):
+def test_fp32_and_fp64_plans_find_the_same_neighbours(cuda, oracle, tmp_path, nb_kernel):
     """Both precisions decide the cut-off with the same FP64 predicate."""
     torch = cuda
     from aenet_gb300 import workloads
