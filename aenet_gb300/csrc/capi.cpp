@@ -793,6 +793,8 @@ struct aenet_gpu_plan {
   double* E_struct = nullptr;
   double* virial = nullptr;
   unsigned* status = nullptr;
+  int nchunks = 0;            // energy-reduction chunks over all structures
+  double2* e_part = nullptr;
   int* order = nullptr;       // atoms grouped by species (tensor-core networks, training)
   int* spec_off = nullptr;    // [AE_MAXT + 1]
   int* part_scratch = nullptr;
@@ -934,7 +936,7 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
 
 int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices) {
   const double rc = P->rc;
-  int cell_off = 0, atom_off = 0;
+  int cell_off = 0, atom_off = 0, nchunks = 0;
   size_t natoms = 0;
   double dens_max = 0;
   for (int s = 0; s < P->nstruc; ++s) {
@@ -946,6 +948,8 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
     int nc = G.nc[0] * G.nc[1] * G.nc[2];
     G.cell_off = cell_off;
     G.atom_off = atom_off;
+    G.chunk_off = nchunks;
+    nchunks += (P->natoms_h[s] + AE_ECHUNK - 1) / AE_ECHUNK;
     cell_off += nc;
     atom_off += P->natoms_h[s];
     natoms += P->natoms_h[s];
@@ -965,6 +969,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   }
   P->natoms = (int)natoms;
   P->ncells = cell_off;
+  P->nchunks = nchunks;
   if (P->cap <= 0) {
     int cap = (int)std::ceil(1.5 * dens_max + 32.0);
     P->cap = (cap + 31) & ~31;
@@ -1015,6 +1020,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_Es = take(8 * (size_t)P->nstruc);
   size_t o_V = take(72 * (size_t)P->nstruc);
   size_t o_st = take(16);
+  size_t o_ep = take(16 * (size_t)(P->nchunks + 1));
   size_t o_ord = take(4 * (size_t)N);
   size_t o_spo = take(4 * (AE_MAXT + 1));
   size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(N));
@@ -1045,6 +1051,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->E_struct = (double*)(b + o_Es);
   P->virial = (double*)(b + o_V);
   P->status = (unsigned*)(b + o_st);
+  P->e_part = (double2*)(b + o_ep);
   P->order = (int*)(b + o_ord);
   P->spec_off = (int*)(b + o_spo);
   P->part_scratch = (int*)(b + o_ps);
@@ -1171,7 +1178,9 @@ int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s)
                                              : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
   if (ck(e)) return AENET_ERR_CUDA;
   if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
-  if (ck(ae_launch_energy_reduce(P->nstruc, P->geom_d, P->E_atom, P->E_struct, s))) return AENET_ERR_CUDA;
+  if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->E_atom, P->e_part,
+                                         P->E_struct, s)))
+    return AENET_ERR_CUDA;
   if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
     return AENET_ERR_CUDA;
   if (d_E_atoms &&
@@ -1868,6 +1877,7 @@ EXPORT int aenet_gpu_plan_set_lattices(aenet_gpu_plan* P, const double* lattices
     if (st) return st;
     G.cell_off = O.cell_off;
     G.atom_off = O.atom_off;
+    G.chunk_off = O.chunk_off;
     O = G;
   }
   if (cudaMemcpy(P->geom_d, P->geom_h.data(), sizeof(StructGeom) * P->nstruc, cudaMemcpyHostToDevice))
@@ -1990,6 +2000,7 @@ struct aenet_gpu_md {
   void* mem = nullptr;
   double *pos = nullptr, *vel = nullptr, *F = nullptr, *S = nullptr, *rb = nullptr,
          *invm = nullptr, *part = nullptr, *scal = nullptr;   // scal: E, E_kin, E_fp64
+  float4* p32 = nullptr;      // positions in the frame of the last build (mixed path)
   int *types = nullptr, *flag = nullptr;
   long long steps = 0;
   int builds = 0;
@@ -2074,7 +2085,7 @@ EXPORT aenet_gpu_md* aenet_gpu_md_create(int natoms, const double* lattice, cons
     return nullptr;
   }
   const size_t N = natoms;
-  const size_t bytes = 8 * (3 * N * 5 + N + ae_md_ekin_blocks() + 4) + 4 * (N + 4) + 256 * 10;
+  const size_t bytes = 8 * (3 * N * 5 + N + ae_md_ekin_blocks() + 4) + 4 * (N + 4) + 16 * N + 256 * 11;
   if (cudaMalloc(&M->mem, bytes)) {
     M->mem = nullptr;
     *stat = AENET_ERR_CUDA;
@@ -2097,6 +2108,7 @@ EXPORT aenet_gpu_md* aenet_gpu_md_create(int natoms, const double* lattice, cons
   M->scal = (double*)take(32);
   M->types = (int*)take(4 * N);
   M->flag = (int*)take(16);
+  M->p32 = (float4*)take(16 * N);
   std::vector<double> invm(N), v0(3 * N, 0.0);
   for (size_t i = 0; i < N; ++i) {
     const int t = type_ids[i];
@@ -2150,9 +2162,12 @@ EXPORT int aenet_gpu_md_run(aenet_gpu_md* M, int nsteps, double* E_pot, double* 
       st = md_build(M);
       P = M->P.get();
     } else {
-      if (ck(ae_md_refresh(M->n, P->geom_d, P->atom_struct, M->pos, M->S, P->cap, P->nb_cnt,
-                           P->nb_jt, P->nb_img, P->nb_vec, P->fp64, s)))
-        return AENET_ERR_CUDA;
+      const int e = P->fp64 ? ae_md_refresh(M->n, P->geom_d, P->atom_struct, M->pos, M->S, P->cap,
+                                            P->nb_cnt, P->nb_jt, P->nb_img, P->nb_vec, 1, s)
+                            : ae_md_refresh_f32(M->n, P->geom_d, P->atom_struct, M->pos, M->S,
+                                                M->p32, P->cap, P->nb_cnt, P->nb_jt, P->nb_img,
+                                                P->nb_vec, s);
+      if (ck(e)) return AENET_ERR_CUDA;
       st = plan_eval(P, nullptr, nullptr, s);
       if (!st) st = plan_adjoint(P, nullptr, M->F, 1.0, nullptr, s);
     }
@@ -2303,7 +2318,8 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   cudaEventRecord(ev[3], s);
   e |= plan_networks(P, d, s);
   cudaEventRecord(ev[4], s);
-  e |= ae_launch_energy_reduce(P->nstruc, P->geom_d, P->E_atom, P->E_struct, s);
+  e |= ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->E_atom, P->e_part,
+                                       P->E_struct, s);
   if (d_E) cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s);
   cudaEventRecord(ev[5], s);
   const size_t tsz = P->fp64 ? 8 : 4;

@@ -168,7 +168,10 @@ struct StructGeom {
   int kr[3];          // stencil half width per axis
   int cell_off;       // first cell of this structure in the global grid
   int atom_off, natoms;
+  int chunk_off;      // first energy-reduction chunk (AE_ECHUNK atoms each)
 };
+
+#define AE_ECHUNK 2048      // atoms per chunk of the per-structure energy sum
 
 // ----------------------------------------------------------------------
 // launchers (defined in the .cu files)
@@ -239,6 +242,11 @@ int ae_launch_mlp_tc(const PotDevice& pd, const DescBuffers& b, const int* order
 int ae_fma_peak(double* tflops, cudaStream_t s);
 int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes,
                     unsigned* status, cudaStream_t s);
+// per-structure energies of large structures: Neumaier sums over chunks of
+// AE_ECHUNK atoms (one warp each), then over each structure's chunks
+int ae_launch_energy_reduce_chunked(int nstruc, int nchunks, const StructGeom* geom,
+                                    const double* E_atom, double2* part, double* E_struct,
+                                    cudaStream_t s);
 int ae_launch_energy_reduce(int nstruc, const StructGeom* geom,
                             const double* E_atom, double* E_struct,
                             cudaStream_t s);
@@ -271,6 +279,9 @@ int ae_md_after_build(int n, const double* pos, const double* r_wrap, double* S,
 int ae_md_refresh(int n, const StructGeom* geom, const int* atom_struct, const double* pos,
                   const double* S, int cap, const int* nb_cnt, const int* nb_jt, const int* nb_img,
                   void* nb_vec, int fp64, cudaStream_t s);
+int ae_md_refresh_f32(int n, const StructGeom* geom, const int* atom_struct, const double* pos,
+                      const double* S, float4* p32, int cap, const int* nb_cnt, const int* nb_jt,
+                      const int* nb_img, void* nb_vec, cudaStream_t s);
 int ae_md_ekin_blocks();
 int ae_md_ekin(int n, const double* vel, const double* invm, double* part, double half_mass_unit,
                double* out, cudaStream_t s);

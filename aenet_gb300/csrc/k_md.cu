@@ -108,6 +108,45 @@ __global__ void k_refresh(int n, const StructGeom* __restrict__ geom, const int*
   }
 }
 
+// FP32 refresh of the mixed path: positions in the frame of the last build
+// rounded to float once per step, vectors formed as the neighbour search
+// forms them, (p_j - p_i) + T L in FP32
+__global__ void k_shifted_f32(int n, const double* __restrict__ pos, const double* __restrict__ S,
+                              float4* __restrict__ p32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  p32[i] = make_float4((float)(pos[3 * i] + S[3 * i]), (float)(pos[3 * i + 1] + S[3 * i + 1]),
+                       (float)(pos[3 * i + 2] + S[3 * i + 2]), 0.f);
+}
+
+__global__ void k_refresh_f32(int n, const StructGeom* __restrict__ geom,
+                              const int* __restrict__ atom_struct, const float4* __restrict__ p32,
+                              int cap, const int* __restrict__ nb_cnt, const int* __restrict__ nb_jt,
+                              const int* __restrict__ nb_img, float4* __restrict__ nb_vec) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const StructGeom& g = geom[atom_struct[i]];
+  const float4 pi = p32[i];
+  const int cnt = nb_cnt[i];
+  const size_t row = (size_t)i * cap;
+  for (int k = lane; k < cnt; k += 32) {
+    const int j = nb_jt[row + k] & AE_INDEX_MASK;
+    const int im = nb_img[row + k];
+    const float f0 = (float)sext10(im & 1023), f1 = (float)sext10((im >> 10) & 1023),
+                f2 = (float)sext10((im >> 20) & 1023);
+    const float4 pj = p32[j];
+    float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
+    if (g.pbc) {
+      sh0 = f0 * g.Lf[0] + f1 * g.Lf[3] + f2 * g.Lf[6];
+      sh1 = f0 * g.Lf[1] + f1 * g.Lf[4] + f2 * g.Lf[7];
+      sh2 = f0 * g.Lf[2] + f1 * g.Lf[5] + f2 * g.Lf[8];
+    }
+    const float dx = (pj.x - pi.x) + sh0, dy = (pj.y - pi.y) + sh1, dz = (pj.z - pi.z) + sh2;
+    nb_vec[row + k] = make_float4(dx, dy, dz, sqrtf(dx * dx + dy * dy + dz * dz));
+  }
+}
+
 // kinetic energy: per-block partial sums (fixed order), then one block
 __global__ void k_ekin_part(int n, const double* __restrict__ vel, const double* __restrict__ invm,
                             double* __restrict__ part) {
@@ -179,6 +218,16 @@ int ae_md_refresh(int n, const StructGeom* geom, const int* atom_struct, const d
   else
     k_refresh<float4><<<blocks, 256, 0, s>>>(n, geom, atom_struct, pos, S, cap, nb_cnt, nb_jt,
                                              nb_img, nb_vec);
+  return (int)cudaGetLastError();
+}
+
+int ae_md_refresh_f32(int n, const StructGeom* geom, const int* atom_struct, const double* pos,
+                      const double* S, float4* p32, int cap, const int* nb_cnt, const int* nb_jt,
+                      const int* nb_img, void* nb_vec, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_shifted_f32<<<(n + 255) / 256, 256, 0, s>>>(n, pos, S, p32);
+  k_refresh_f32<<<(int)(((size_t)n * 32 + 255) / 256), 256, 0, s>>>(
+      n, geom, atom_struct, p32, cap, nb_cnt, nb_jt, nb_img, reinterpret_cast<float4*>(nb_vec));
   return (int)cudaGetLastError();
 }
 

@@ -173,6 +173,76 @@ __global__ void k_energy_reduce(int nstruc, const StructGeom* geom, const double
   if (lane == 0) E_struct[sidx] = s + c;
 }
 
+// chunk c of the structure whose chunk range contains it
+__global__ void k_energy_chunks(int nstruc, int nchunks, const StructGeom* __restrict__ geom,
+                                const double* __restrict__ E_atom, double2* __restrict__ part,
+                                double* __restrict__ E_struct) {
+  const int lane = threadIdx.x & 31;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (c >= nchunks) return;
+  int lo = 0, hi = nstruc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (geom[mid].chunk_off <= c) lo = mid; else hi = mid - 1;
+  }
+  const StructGeom& g = geom[lo];
+  const int a0 = (c - g.chunk_off) * AE_ECHUNK;
+  const int a1 = min(g.natoms, a0 + AE_ECHUNK);
+  double s = 0.0, e = 0.0;
+  for (int a = a0 + lane; a < a1; a += 32) {
+    double t, r;
+    two_sum(s, E_atom[g.atom_off + a], t, r);
+    s = t;
+    e += r;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const double so = __shfl_xor_sync(0xffffffffu, s, d);
+    const double eo = __shfl_xor_sync(0xffffffffu, e, d);
+    double t, r;
+    two_sum(s, so, t, r);
+    s = t;
+    e = e + eo + r;
+  }
+  if (lane == 0) {
+    part[c] = make_double2(s, e);
+    if (g.natoms <= AE_ECHUNK) E_struct[lo] = s + e;   // single chunk: final already
+  }
+}
+
+// one warp per structure over its chunks
+__global__ void k_energy_struct(int nstruc, int nchunks, const StructGeom* __restrict__ geom,
+                                const double2* __restrict__ part, double* __restrict__ E_struct) {
+  const int lane = threadIdx.x & 31;
+  const int sidx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (sidx >= nstruc) return;
+  const int c0 = geom[sidx].chunk_off;
+  const int c1 = sidx + 1 < nstruc ? geom[sidx + 1].chunk_off : nchunks;
+  if (c1 - c0 == 1) return;   // written by k_energy_chunks
+  if (c1 == c0) {
+    if (lane == 0) E_struct[sidx] = 0.0;
+    return;
+  }
+  double s = 0.0, e = 0.0;
+  for (int c = c0 + lane; c < c1; c += 32) {
+    const double2 p = part[c];
+    double t, r;
+    two_sum(s, p.x, t, r);
+    s = t;
+    e += r + p.y;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const double so = __shfl_xor_sync(0xffffffffu, s, d);
+    const double eo = __shfl_xor_sync(0xffffffffu, e, d);
+    double t, r;
+    two_sum(s, so, t, r);
+    s = t;
+    e = e + eo + r;
+  }
+  if (lane == 0) E_struct[sidx] = s + e;
+}
+
 template <typename T>
 __global__ void k_forces_out(int natoms, const T* __restrict__ Facc, double* __restrict__ F,
                              double f) {
@@ -273,6 +343,17 @@ int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStrea
       cudaFuncSetAttribute(k_mlp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_mlp<float><<<blocks, warps * 32, smem, s>>>(pd, b, pd.w32, wtotal);
   }
+  return (int)cudaGetLastError();
+}
+
+int ae_launch_energy_reduce_chunked(int nstruc, int nchunks, const StructGeom* geom,
+                                    const double* E_atom, double2* part, double* E_struct,
+                                    cudaStream_t s) {
+  if (nstruc <= 0) return 0;
+  if (nchunks > 0)
+    k_energy_chunks<<<(nchunks + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, E_atom, part,
+                                                      E_struct);
+  k_energy_struct<<<(nstruc + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, part, E_struct);
   return (int)cudaGetLastError();
 }
 

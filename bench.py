@@ -75,7 +75,8 @@ def load_workload(args, rank):
     """The seeded batch; cached (structures and network weights) on disk
     because the random placement takes a few seconds."""
     from aenet_gb300 import nnfile, workloads
-    seed = args.seed + 1000 * rank
+    from aenet_gb300.replicas import replica_seed
+    seed = replica_seed(args.seed, rank)
     os.makedirs(args.cache, exist_ok=True)
     f = os.path.join(args.cache, "lisio_%d_%d.npz" % (seed, args.nstruc))
     if os.path.exists(f):
@@ -335,12 +336,11 @@ def run_gb300(args):
     total_ms, wall = timed(plan32, out32, args.steps, g32)
     clocks = sampler.stop()
     plan32.check()
-    tmax = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-    total_ms = float(tmax.item())
+    from aenet_gb300.replicas import job_rate, max_over_ranks
+    # every rank evaluates its own batch: total atoms over the slowest rank
+    value = job_rate(N, total_ms * 1e-3 / args.steps, device=dev)
+    total_ms = max_over_ranks(total_ms, device=dev)
     ms_step = total_ms / args.steps
-    value = world * N / (ms_step * 1e-3)
     res32 = {k: v.clone() for k, v in out32.items()}
 
     # ---- stage profile and roofline of the dominant kernel
@@ -398,7 +398,7 @@ def run_gb300(args):
     plan64, out64, g64 = prepare(FP64)
     ms64, _ = timed(plan64, out64, max(1, args.fp64_steps), g64)
     ms64 /= max(1, args.fp64_steps)
-    value64 = world * N / (ms64 * 1e-3)
+    value64 = job_rate(N, ms64 * 1e-3, device=dev)
     natoms_t = torch.tensor(nat, device=dev, dtype=torch.float64)
     dE = ((res32["E"] - out64["E"]).abs() / natoms_t)
     dF = res32["F"] - out64["F"]
@@ -443,10 +443,9 @@ def run_gb300(args):
             call()
             calls.append(time.perf_counter() - t0)
         e2e_s = float(np.mean(calls))
-        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * N / tt.item(), "unit": "atoms/s",
+        e2e_rate = job_rate(N, e2e_s, device=dev)
+        tt = torch.tensor([max_over_ranks(e2e_s, device=dev)], dtype=torch.float64)
+        e2e = {"value": e2e_rate, "unit": "atoms/s",
                "h2d_bytes_per_step": N * 24 + N * 4, "d2h_bytes_per_step": S * 8 + N * 24,
                "ms_per_step": 1e3 * tt.item(), "api": "aenet_gpu_batch_energy_forces"}
         # same kernels, neighbour order within a cell may differ: FP32 noise
@@ -551,6 +550,11 @@ def run_md(args, local):
     ann = ANNPotentials(paths)
     s = w.structures[0]
     try:
+        tuned = None
+        if not args.no_tune:
+            from aenet_gb300 import autotune
+            tuned = autotune.tune(np.array([s.natoms]), s.cell[None], np.array([1]), s.positions,
+                                  s.types, precision=MIXED, cache=None)
         md = MolecularDynamics(ann, s.positions, s.types, s.cell, velocities=w.velocities,
                                dt=2.0, skin=0.3, precision=MIXED)
         e0 = md.E_pot + md.E_kin
@@ -576,7 +580,8 @@ def run_md(args, local):
                "fp64_monitor_max_eV_per_atom": max(monitor),
                "energy_drift_max_eV_per_atom": max(drift),
                "timing": "host wall clock around md.run blocks of 10 steps (one sync per "
-                         "step for the skin check), FP64 monitor outside"}
+                         "step for the skin check), FP64 monitor outside",
+               "launch_shape": tuned}
         md.close()
     finally:
         ann.release()
