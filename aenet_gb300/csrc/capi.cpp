@@ -925,6 +925,10 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
     }
   }
   for (int q = 0; q < 9; ++q) G.Lf[q] = (float)G.L[q];
+  for (int c = 0; c < 3; ++c) {
+    G.inv_nc[c] = 1.0f / (float)G.nc[c];
+    G.inv_hf[c] = 1.0f / G.hf[c];
+  }
   // FP32 distances carry an error below ~1e-6 ext per component; the band
   // is four times the resulting bound on d^2
   double err = 4.0 * (2.0 * rcp * 4.0e-7 * ext + 1.0e-6 * G.rc2);

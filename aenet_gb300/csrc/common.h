@@ -157,6 +157,8 @@ struct StructGeom {
   double box[3];      // isolated structures: edge lengths of the box
   float Lf[9];
   float hf[3];        // heights of the cell (periodic) or box edges
+  float inv_nc[3];    // 1 / nc and 1 / hf, so the search kernels multiply
+  float inv_hf[3];
   double rc2;         // (Rc + 1e-3)^2, the neighbour predicate
   float rc2_lo, rc2_hi;   // FP32 distances in [lo, hi] are decided in FP64
   float rcf;          // Rc + 1e-3 (pruning of the cell stencil)

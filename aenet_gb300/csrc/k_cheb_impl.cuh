@@ -23,11 +23,12 @@
 //   radial:  dE/dd_ij = sum_n g_n (fc' T_n + fc T_n')       along R_ij/d_ij
 //   angular: E_jk = w A(cos), w = fc_j fc_k, A = sum_n g_n T_n
 //            grad_j E_jk = fc_j' fc_k A Rhat_j + w A' (Rhat_k - cos Rhat_j)/d_j
-// In the adjoint the angular term is evaluated two-sided: the lane owning a
-// staged neighbour sweeps all partners and accumulates only that
-// neighbour's gradient, so forces stay in registers (no shared-memory
-// atomics); each neighbour's force is scattered once; the central atom
-// receives minus the sum.
+// In the adjoint every angular pair is evaluated once, on a circulant
+// schedule (the owner of staged neighbour a takes partners a + t mod na,
+// t = 1 .. na/2): the lanes of a group always touch distinct partners, so
+// partner forces accumulate in shared memory without atomics and the
+// owner's in registers; each neighbour's force is scattered to global
+// memory once; the central atom receives minus the sum.
 #pragma once
 #include "common.h"
 
@@ -478,10 +479,13 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
   }
   __syncwarp();
 
-  // ---- angular terms, two-sided: the lane that owns staged neighbour a
-  // sweeps every partner k != a (all lanes of a group read the same k, a
-  // shared-memory broadcast) and accumulates only grad_a of E_ak, so no
-  // force is ever written by two lanes.
+  // ---- angular terms, one-sided on a circulant schedule: the lane that
+  // owns staged neighbour a evaluates the pairs (a, k = a + t mod na) for
+  // t = 1 .. na/2 (t = na/2 only from the lower half when na is even), so
+  // every pair is evaluated once.  At each step the lanes of a group touch
+  // distinct partners k, so the partner's force is added to shared memory
+  // without atomics; a's own gradient stays in registers until the end of
+  // its round.
   const T* ga = sm.g + ct.a_i1;
   const T* gas = sm.g + ct.a_i2;
   T gav[A], gasv[A];
@@ -490,8 +494,8 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
     gav[q] = (!GUARD || q < aN) ? ga[q] : T(0);
     gasv[q] = (multi && (!GUARD || q < aN)) ? gas[q] : T(0);
   }
-  const int naloop = warp_max(na);
-  for (int a0 = 0; a0 < naloop; a0 += LPA) {
+  const int tmax = na / 2;
+  for (int a0 = 0; a0 < na; a0 += LPA) {
     const int a = a0 + sl;
     const bool own = active && a < na;
     T4 ua, fa;
@@ -504,9 +508,11 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
       fa.x = fa.y = fa.z = fa.w = T(0);
     }
     const T inva = T(1) / ua.w;
-    T gx = T(0), gy = T(0), gz = T(0);
-    for (int k = 0; k < naloop; ++k) {
-      if (own && k < na && k != a) {
+    T gax = T(0), gay = T(0), gaz = T(0);
+    for (int t = 1; t <= tmax; ++t) {
+      int k = a + t;
+      if (k >= na) k -= na;
+      if (own && !(2 * t == na && a >= tmax)) {
         const T4 uk = sm.au[k];
         const T4 fk = sm.af[k];
         const T cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
@@ -516,15 +522,13 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
         angular_arg(cosv, ct.angular_legacy, x, dxdc);
         const T x2 = x + x;
         T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
-        T Av = gav[0], As = gasv[0], Bv = T(0), Bs = T(0);
+        T Av = fma(ss, gasv[0], gav[0]), Bv = T(0);
 #pragma unroll
         for (int q = 1; q < A; ++q) {
           if (!GUARD || q < aN) {
-            Av = fma(gav[q], t0, Av);
-            As = fma(gasv[q], t0, As);
-            const T dq = T(q) * um1;
-            Bv = fma(gav[q], dq, Bv);
-            Bs = fma(gasv[q], dq, Bs);
+            const T cq = fma(ss, gasv[q], gav[q]);
+            Av = fma(cq, t0, Av);
+            Bv = fma(cq * T(q), um1, Bv);
             const T tn = fma(x2, t0, -tm1);
             tm1 = t0;
             t0 = tn;
@@ -533,28 +537,46 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
             u0 = un;
           }
         }
-        Av = fma(ss, As, Av);
-        Bv = fma(ss, Bs, Bv);
-        const T dEda = fa.y * fk.x * Av;         // d/dd_a of w A
-        const T dEdc = w * Bv * dxdc * inva;     // (dE/dcos) / d_a
-        gx += dEda * ua.x + dEdc * (uk.x - cosv * ua.x);
-        gy += dEda * ua.y + dEdc * (uk.y - cosv * ua.y);
-        gz += dEda * ua.z + dEdc * (uk.z - cosv * ua.z);
+        const T invk = T(1) / uk.w;
+        const T Bc = w * Bv * dxdc;
+        const T dEda = fa.y * fk.x * Av, ca = Bc * inva;   // d/dd_a of w A, (dE/dcos)/d_a
+        const T dEdk = fa.x * fk.y * Av, ck = Bc * invk;
+        const T gx = dEda * ua.x + ca * (uk.x - cosv * ua.x);
+        const T gy = dEda * ua.y + ca * (uk.y - cosv * ua.y);
+        const T gz = dEda * ua.z + ca * (uk.z - cosv * ua.z);
+        const T hx = dEdk * uk.x + ck * (ua.x - cosv * uk.x);
+        const T hy = dEdk * uk.y + ck * (ua.y - cosv * uk.y);
+        const T hz = dEdk * uk.z + ck * (ua.z - cosv * uk.z);
+        gax += gx;
+        gay += gy;
+        gaz += gz;
+        sm.fbuf[3 * k] -= hx;
+        sm.fbuf[3 * k + 1] -= hy;
+        sm.fbuf[3 * k + 2] -= hz;
+        fix += gx + hx;
+        fiy += gy + hy;
+        fiz += gz + hz;
       }
+      __syncwarp(gmask);
     }
     if (own) {
-      const int slot = (int)fa.w;
-      const T fx = sm.fbuf[3 * a] - gx, fy = sm.fbuf[3 * a + 1] - gy, fz = sm.fbuf[3 * a + 2] - gz;
-      atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
-      if (want_virial) {
-        const T4 v = vec[slot];
-        w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
-        w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
-        w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
-      }
-      fix += gx;
-      fiy += gy;
-      fiz += gz;
+      sm.fbuf[3 * a] -= gax;
+      sm.fbuf[3 * a + 1] -= gay;
+      sm.fbuf[3 * a + 2] -= gaz;
+    }
+    __syncwarp(gmask);
+  }
+  // forces on the staged neighbours (radial + angular), one scatter each
+  for (int a = sl; a < na; a += LPA) {
+    if (!active) break;
+    const int slot = (int)sm.af[a].w;
+    const T fx = sm.fbuf[3 * a], fy = sm.fbuf[3 * a + 1], fz = sm.fbuf[3 * a + 2];
+    atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
+    if (want_virial) {
+      const T4 v = vec[slot];
+      w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
+      w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
+      w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
     }
   }
   fix = gsum<T, LPA>(fix);

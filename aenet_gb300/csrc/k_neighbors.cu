@@ -180,6 +180,12 @@ __global__ void k_scatter(int natoms, NbBuffers nb) {
 
 __device__ __forceinline__ int sext10i(int v) { return (v ^ 512) - 512; }
 
+// floor(a / n) for |a| < 2^20 with a reciprocal: (a + 1/2) / n is at least
+// 1/(2n) away from an integer, far more than the rounding of the product
+__device__ __forceinline__ int floor_div_r(int a, float inv_n) {
+  return (int)floorf(((float)a + 0.5f) * inv_n);
+}
+
 __device__ __forceinline__ int floor_div(int a, int n) {
   int q = a / n;
   return (a % n != 0 && (a < 0)) ? q - 1 : q;
@@ -226,37 +232,45 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
   const float rcf = g->rcf * 1.0001f + 1e-4f;
   int cnt = 0;
 
+  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
+  // geometry in registers: the table stores below may alias g as far as
+  // the compiler knows, which would otherwise reload these every unit
+  const int ortho = g->ortho;
+  const float hf0 = g->hf[0], hf1 = g->hf[1], ihf2 = g->inv_hf[2];
+  const float* __restrict__ Lf = g->Lf;
   for (int ubase = 0; ubase < nunits; ubase += 32) {
     // ---- this lane's unit: cells [zlo, zhi] of row (d0, d1), image t2
     const int u = ubase + lane;
     int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
     float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
     if (u < nunits) {
-      const int it2 = u % nt2;
-      const int rr = u / nt2;
-      const int d1 = rr % w1 - k1;
-      const int d0 = rr / w1 - k0;
+      const int rr = floor_div_r(u, inv_nt2);
+      const int it2 = u - rr * nt2;
+      const int q0 = floor_div_r(rr, inv_w1);
+      const int d1 = rr - q0 * w1 - k1;
+      const int d0 = q0 - k0;
       int a0 = c0 + d0, a1 = c1 + d1;
       bool ok = true;
       int zlo = c2 - k2, zhi = c2 + k2;   // unwrapped cell indices
-      if (g->ortho) {
-        const float x0 = (float)a0 / nc0, x1 = (float)(a0 + 1) / nc0;
-        const float y0 = (float)a1 / nc1, y1 = (float)(a1 + 1) / nc1;
-        const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * g->hf[0];
-        const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * g->hf[1];
+      if (ortho) {
+        const float x0 = (float)a0 * inc0, x1 = (float)(a0 + 1) * inc0;
+        const float y0 = (float)a1 * inc1, y1 = (float)(a1 + 1) * inc1;
+        const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * hf0;
+        const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * hf1;
         const float rem = rcf * rcf - gx * gx - gy * gy;
         if (rem < 0.f) {
           ok = false;
         } else {
-          const float hz = sqrtf(rem) / g->hf[2] * 1.0001f + 1e-6f;
+          const float hz = sqrtf(rem) * ihf2 * 1.0001f + 1e-6f;
           zlo = max(zlo, (int)floorf((sf2 - hz) * nc2));
           zhi = min(zhi, (int)floorf((sf2 + hz) * nc2));
         }
       }
       if (pbc) {
-        T0 = floor_div(a0, nc0);
+        T0 = floor_div_r(a0, inc0);
         a0 -= T0 * nc0;
-        T1 = floor_div(a1, nc1);
+        T1 = floor_div_r(a1, inc1);
         a1 -= T1 * nc1;
         T2 = t2lo + it2;
         zlo = max(zlo, T2 * nc2);
@@ -271,9 +285,9 @@ __global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
         beg = cstart[base + zlo];
         len = cstart[base + zhi + 1] - beg;
         const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
-        sh0 = f0 * g->Lf[0] + f1 * g->Lf[3] + f2 * g->Lf[6];
-        sh1 = f0 * g->Lf[1] + f1 * g->Lf[4] + f2 * g->Lf[7];
-        sh2 = f0 * g->Lf[2] + f1 * g->Lf[5] + f2 * g->Lf[8];
+        sh0 = f0 * Lf[0] + f1 * Lf[3] + f2 * Lf[6];
+        sh1 = f0 * Lf[1] + f1 * Lf[4] + f2 * Lf[7];
+        sh2 = f0 * Lf[2] + f1 * Lf[5] + f2 * Lf[8];
       }
     }
     int incl = len;
@@ -435,6 +449,7 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
   const int cap = nb.cap;
   const int* __restrict__ cstart = nb.cell_start + g->cell_off;
   const float rcf = g->rcf * 1.0001f + 1e-4f;
+  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
 
   for (int hbase = hb; hbase < he; hbase += 32) {
     const bool home = hbase + lane < he;
@@ -447,30 +462,31 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
       int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
       float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
       if (u < nunits) {
-        const int it2 = u % nt2;
-        const int rr = u / nt2;
-        const int d1 = rr % w1 - k1;
-        const int d0 = rr / w1 - k0;
+        const int rr = floor_div_r(u, inv_nt2);
+        const int it2 = u - rr * nt2;
+        const int q0 = floor_div_r(rr, inv_w1);
+        const int d1 = rr - q0 * w1 - k1;
+        const int d0 = q0 - k0;
         int a0 = c0 + d0, a1 = c1 + d1;
         bool ok = true;
         int zlo = c2 - k2, zhi = c2 + k2;
         if (g->ortho) {
           // gap between the home cell and row (a0, a1), whole cells apart
-          const float gx = (float)max(0, abs(d0) - 1) * g->hf[0] / nc0;
-          const float gy = (float)max(0, abs(d1) - 1) * g->hf[1] / nc1;
+          const float gx = (float)max(0, abs(d0) - 1) * g->hf[0] * g->inv_nc[0];
+          const float gy = (float)max(0, abs(d1) - 1) * g->hf[1] * g->inv_nc[1];
           const float rem = rcf * rcf - gx * gx - gy * gy;
           if (rem < 0.f) {
             ok = false;
           } else {
-            const int hz = 1 + (int)floorf(sqrtf(rem) / g->hf[2] * nc2 * 1.0001f + 1e-4f);
+            const int hz = 1 + (int)floorf(sqrtf(rem) * g->inv_hf[2] * nc2 * 1.0001f + 1e-4f);
             zlo = max(zlo, c2 - hz);
             zhi = min(zhi, c2 + hz);
           }
         }
         if (pbc) {
-          T0 = floor_div(a0, nc0);
+          T0 = floor_div_r(a0, g->inv_nc[0]);
           a0 -= T0 * nc0;
-          T1 = floor_div(a1, nc1);
+          T1 = floor_div_r(a1, g->inv_nc[1]);
           a1 -= T1 * nc1;
           T2 = t2lo + it2;
           zlo = max(zlo, T2 * nc2);
