@@ -104,6 +104,9 @@ def _declare(lib):
     lib.aenet_gpu_set_weights.restype = C.c_int
     lib.aenet_gpu_save_potential.argtypes = [C.c_int, C.c_char_p]
     lib.aenet_gpu_save_potential.restype = C.c_int
+    lib.aenet_gpu_neighbor_list_energy_forces.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, C.c_int,
+                                                           vp, vp, vp, vp]
+    lib.aenet_gpu_neighbor_list_energy_forces.restype = C.c_int
     lib.aenet_gpu_md_create.argtypes = [C.c_int, vp, vp, vp, vp, vp, C.c_double, C.c_double,
                                         C.c_int, ip]
     lib.aenet_gpu_md_create.restype = vp

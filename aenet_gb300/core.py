@@ -245,6 +245,30 @@ class ANNPotentials:
             out["virial"] = W
         return out
 
+    def neighbor_list_energy_forces(self, x, types, neigh_offset, neighbors, nlocal,
+                                    precision=MIXED, virial=False):
+        """Energy and forces from a caller's neighbour list: ``x`` holds the
+        ``nlocal`` local atoms then the ghosts, ``neigh_offset``/``neighbors``
+        the CSR lists of the local atoms.  Forces are returned for all atoms
+        (ghosts included)."""
+        x = _f64(x).reshape(-1, 3)
+        nall = x.shape[0]
+        t = self._types(types)
+        off = _i32(neigh_offset)
+        nb = _i32(neighbors)
+        E = C.c_double(0.0)
+        Ea = np.zeros(nlocal)
+        F = np.zeros((nall, 3))
+        W = np.zeros((3, 3)) if virial else None
+        st = _lib.lib().aenet_gpu_neighbor_list_energy_forces(
+            int(nlocal), nall, _ptr(x), _ptr(t), _ptr(off), _ptr(nb) if nb.size else None,
+            int(precision), C.byref(E), _ptr(Ea), _ptr(F), _ptr(W))
+        check_status(st)
+        out = {"energy": E.value, "atomic_energies": Ea, "forces": F}
+        if virial:
+            out["virial"] = W
+        return out
+
     def _types(self, symbols_or_types):
         a = np.asarray(symbols_or_types)
         if a.dtype.kind in "iu":

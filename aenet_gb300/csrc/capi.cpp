@@ -835,6 +835,7 @@ struct HostPlanCache {
   }
 };
 HostPlanCache g_cache;
+void nlist_release();   // drops the neighbour-list entry point's workspace
 }  // namespace
 
 namespace {
@@ -1248,6 +1249,7 @@ EXPORT void aenet_final(int* stat) {
   *stat = AENET_OK;
   if (g.init) {
     g_cache.reset();
+    nlist_release();
     g.blob.reset();
     g.pots.clear();
     g.types.clear();
@@ -2226,6 +2228,166 @@ EXPORT int aenet_gpu_md_energy_fp64(aenet_gpu_md* M, double* E) {
   if (cudaMemcpyAsync(E, M->scal + 2, 8, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
     return AENET_ERR_CUDA;
   return AENET_OK;
+}
+
+// ---- caller's neighbour lists (MD engines) ---------------------------
+
+namespace {
+struct NlistCtx {
+  std::unique_ptr<aenet_gpu_plan> P;
+  int nlocal = -1, nall = -1, cap = 0, cap_a = 0, precision = -1;
+  size_t nnz_cap = 0;
+  void* io = nullptr;
+  size_t io_bytes = 0;
+  double* x = nullptr;
+  int* types = nullptr;
+  int* offs = nullptr;
+  int* nbr = nullptr;
+  void* Facc = nullptr;
+  double* F = nullptr;
+  double* E = nullptr;
+  double* Ea = nullptr;
+  double* V = nullptr;
+  cudaStream_t stream = nullptr;
+  ~NlistCtx() {
+    if (io) cudaFree(io);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+std::unique_ptr<NlistCtx> g_nlist;
+void nlist_release() { g_nlist.reset(); }
+
+int nlist_setup(NlistCtx& c, int nlocal, int nall, const double* x, size_t nnz, int cap, int cap_a,
+                int precision) {
+  if (!c.stream && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) return AENET_ERR_CUDA;
+  if (!c.P || c.nlocal != nlocal || c.precision != precision || cap > c.cap || cap_a != c.cap_a) {
+    int st = 0;
+    const int pbc = 0;
+    c.P.reset(plan_new(1, &nlocal, nullptr, &pbc, x, precision, &g.pd, aenet_Rc_max, cap, false, &st));
+    if (!c.P) return st ? st : AENET_ERR_CUDA;
+    c.P->cap_a = std::min(cap_a, c.P->cap);
+    c.nlocal = nlocal;
+    c.precision = precision;
+    c.cap = c.P->cap;
+    c.cap_a = cap_a;
+    c.nall = -1;
+  }
+  const size_t tsz = precision == AENET_GPU_FP64 ? 8 : 4;
+  if (c.nall != nall || nnz > c.nnz_cap) {
+    if (c.io) cudaFree(c.io);
+    c.io = nullptr;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+      size_t o = off;
+      off = (off + b + 255) & ~(size_t)255;
+      return o;
+    };
+    const size_t NA = nall, NL = nlocal;
+    size_t o_x = take(24 * NA), o_t = take(4 * NA), o_o = take(4 * (NL + 1)), o_n = take(4 * nnz + 4);
+    size_t o_fa = take(4 * tsz * NA), o_f = take(24 * NA), o_e = take(8), o_ea = take(8 * NL + 8),
+           o_v = take(72);
+    if (cudaMalloc(&c.io, off)) {
+      c.io = nullptr;
+      return AENET_ERR_CUDA;
+    }
+    char* b = (char*)c.io;
+    c.x = (double*)(b + o_x);
+    c.types = (int*)(b + o_t);
+    c.offs = (int*)(b + o_o);
+    c.nbr = (int*)(b + o_n);
+    c.Facc = (void*)(b + o_fa);
+    c.F = (double*)(b + o_f);
+    c.E = (double*)(b + o_e);
+    c.Ea = (double*)(b + o_ea);
+    c.V = (double*)(b + o_v);
+    c.nall = nall;
+    c.nnz_cap = nnz;
+  }
+  return 0;
+}
+}  // namespace
+
+// Energy and forces from the caller's neighbour list (see aenet_gb300.h).
+EXPORT int aenet_gpu_neighbor_list_energy_forces(int nlocal, int nall, const double* x,
+                                                 const int* type_ids, const int* neigh_offset,
+                                                 const int* neighbors, int precision,
+                                                 double* E_total, double* E_atoms, double* F,
+                                                 double* virial) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g.init || !g.loaded) return AENET_ERR_INIT;
+  if (nlocal < 1 || nall < nlocal || !x || !type_ids || !neigh_offset ||
+      (precision != AENET_GPU_FP64 && precision != AENET_GPU_MIXED))
+    return AENET_ERR_INPUT;
+  int st = ensure_device();
+  if (st) return st;
+  const size_t nnz = (size_t)neigh_offset[nlocal];
+  if (neigh_offset[0] != 0 || (nnz && !neighbors)) return AENET_ERR_INPUT;
+  int cap = 0;
+  for (int i = 0; i < nlocal; ++i) {
+    const int n = neigh_offset[i + 1] - neigh_offset[i];
+    if (n < 0) return AENET_ERR_INPUT;
+    cap = std::max(cap, n);
+  }
+  cap = ((cap + 31) & ~31) + 32;
+  // staged angular neighbours: the share of the cut-off sphere inside the
+  // largest angular cut-off, with room to spare; all of them on a retry
+  double arc = 0.0;
+  for (int t = 0; t < g.pd.ntypes; ++t)
+    arc = std::max(arc, g.pd.sp[t].sftype == AE_SF_CHEBYSHEV ? g.pd.sp[t].cheb.a_Rc : aenet_Rc_max);
+  const double frac = std::pow(std::min(1.0, (arc + 1e-3) / (aenet_Rc_max + 1e-3)), 3);
+  int cap_a = std::min(cap, (((int)std::ceil(1.5 * frac * cap) + 16) + 7) & ~7);
+  if (!g_nlist) g_nlist = std::make_unique<NlistCtx>();
+  NlistCtx& c = *g_nlist;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    st = nlist_setup(c, nlocal, nall, x, nnz, cap, cap_a, precision);
+    if (st) {
+      g_nlist.reset();
+      return st;
+    }
+    aenet_gpu_plan* P = c.P.get();
+    cudaStream_t s = c.stream;
+    const size_t tsz = P->fp64 ? 8 : 4;
+    const double rcp = aenet_Rc_max + 1.0e-3;
+    if (cudaMemcpyAsync(c.x, x, 24 * (size_t)nall, cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(c.types, type_ids, 4 * (size_t)nall, cudaMemcpyHostToDevice, s) ||
+        cudaMemcpyAsync(c.offs, neigh_offset, 4 * ((size_t)nlocal + 1), cudaMemcpyHostToDevice, s) ||
+        (nnz && cudaMemcpyAsync(c.nbr, neighbors, 4 * nnz, cudaMemcpyHostToDevice, s)) ||
+        cudaMemsetAsync(P->status, 0, 4, s))
+      return AENET_ERR_CUDA;
+    const PotDevice& pd = *P->pd;
+    if (ck(ae_launch_types(nlocal, c.types, P->types0, pd.ntypes, P->status, s)) ||
+        ck(ae_launch_ell_from_csr(nlocal, nall, c.x, c.types, pd.ntypes, c.offs, c.nbr, rcp * rcp,
+                                  P->cap, P->nb_cnt, P->nb_jt, P->nb_vec, P->fp64, P->status, s)))
+      return AENET_ERR_CUDA;
+    st = plan_eval(P, c.E, c.Ea, s);
+    if (st) return st;
+    if (cudaMemsetAsync(c.Facc, 0, 4 * tsz * (size_t)nall, s) ||
+        cudaMemsetAsync(P->virial, 0, 72, s))
+      return AENET_ERR_CUDA;
+    DescBuffers d = desc_buffers(P, nullptr, true);
+    d.F = c.Facc;
+    int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, P->fp64, s)
+                                               : ae_launch_chebyshev_adjoint(pd, d, P->fp64, s);
+    if (ck(e) || ck(ae_launch_forces_out(nall, c.Facc, P->fp64, c.F, 1.0, s))) return AENET_ERR_CUDA;
+    unsigned status = 0;
+    double Et = 0.0;
+    if (cudaMemcpyAsync(&status, P->status, 4, cudaMemcpyDeviceToHost, s) ||
+        cudaMemcpyAsync(&Et, c.E, 8, cudaMemcpyDeviceToHost, s) ||
+        (E_atoms && cudaMemcpyAsync(E_atoms, c.Ea, 8 * (size_t)nlocal, cudaMemcpyDeviceToHost, s)) ||
+        (F && cudaMemcpyAsync(F, c.F, 24 * (size_t)nall, cudaMemcpyDeviceToHost, s)) ||
+        (virial && cudaMemcpyAsync(virial, P->virial, 72, cudaMemcpyDeviceToHost, s)) ||
+        cudaStreamSynchronize(s))
+      return AENET_ERR_CUDA;
+    if (status & AE_ST_BAD_TYPE) return AENET_ERR_TYPE;
+    if (status & AE_ST_TC_TIMEOUT) return AENET_ERR_CUDA;
+    if (status & AE_ST_NB_OVERFLOW) {
+      cap_a = cap;   // stage every neighbour
+      continue;
+    }
+    if (E_total) *E_total = Et;
+    return AENET_OK;
+  }
+  return AENET_ERR_MALLOC;
 }
 
 // ---- network weights ------------------------------------------------

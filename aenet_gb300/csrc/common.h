@@ -204,6 +204,11 @@ struct NbBuffers {
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types,
                         const NbBuffers& nb, int fp64, cudaStream_t s);
+// ELL table from a caller's CSR neighbour list (local atoms, indices into
+// local + ghost atoms)
+int ae_launch_ell_from_csr(int nlocal, int nall, const double* x, const int* types1, int ntypes,
+                           const int* offs, const int* nbr, double rc2, int cap, int* nb_cnt,
+                           int* nb_jt, void* nb_vec, int fp64, unsigned* status, cudaStream_t s);
 
 struct DescBuffers {
   int natoms;

@@ -630,7 +630,80 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
   }
 }
 
+// ---- caller's neighbour list (CSR over local atoms, indices into local +
+// ghost atoms) -> ELL table.  R_ij = x_j - x_i in FP64; pairs beyond
+// (Rc + 1e-3) are dropped; species from the caller's type ids.
+template <typename T4>
+__global__ void k_ell_from_csr(int nlocal, int nall, const double* __restrict__ x,
+                               const int* __restrict__ types1, int ntypes,
+                               const int* __restrict__ offs, const int* __restrict__ nbr,
+                               double rc2, int cap, int* __restrict__ nb_cnt,
+                               int* __restrict__ nb_jt, void* nb_vec, unsigned* status) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= nlocal) return;
+  const double xi0 = x[3 * i], xi1 = x[3 * i + 1], xi2 = x[3 * i + 2];
+  const int b0 = offs[i], b1 = offs[i + 1];
+  const size_t row = (size_t)i * cap;
+  int cnt = 0;
+  for (int base = b0; base < b1; base += 32) {
+    const int q = base + lane;
+    bool accept = false;
+    int j = 0, tj = 0;
+    double R0 = 0, R1 = 0, R2 = 0, d2 = 0;
+    if (q < b1) {
+      j = nbr[q];
+      if (j >= 0 && j < nall && j != i) {
+        R0 = da(x[3 * j], -xi0);
+        R1 = da(x[3 * j + 1], -xi1);
+        R2 = da(x[3 * j + 2], -xi2);
+        d2 = da(da(dm(R0, R0), dm(R1, R1)), dm(R2, R2));
+        tj = types1[j] - 1;
+        if (tj < 0 || tj >= ntypes) {
+          atomicOr(status, AE_ST_BAD_TYPE);
+          tj = 0;
+        }
+        accept = d2 <= rc2;
+      } else if (j < 0 || j >= nall) {
+        atomicOr(status, AE_ST_BAD_TYPE);
+      }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, accept);
+    if (accept) {
+      const int k = cnt + __popc(mask & ((1u << lane) - 1u));
+      if (k < cap) {
+        nb_jt[row + k] = j | (tj << AE_TYPE_SHIFT);
+        const double d = sqrt(d2);
+        if (VecOut<T4>::fp64)
+          reinterpret_cast<double4_32a*>(nb_vec)[row + k] = make_double4_32a(R0, R1, R2, d);
+        else
+          reinterpret_cast<float4*>(nb_vec)[row + k] =
+              make_float4((float)R0, (float)R1, (float)R2, (float)d);
+      }
+    }
+    cnt += __popc(mask);
+  }
+  if (lane == 0) {
+    nb_cnt[i] = min(cnt, cap);
+    if (cnt > cap) atomicOr(status, AE_ST_NB_OVERFLOW);
+  }
+}
+
 }  // namespace
+
+int ae_launch_ell_from_csr(int nlocal, int nall, const double* x, const int* types1, int ntypes,
+                           const int* offs, const int* nbr, double rc2, int cap, int* nb_cnt,
+                           int* nb_jt, void* nb_vec, int fp64, unsigned* status, cudaStream_t s) {
+  if (nlocal <= 0) return 0;
+  const int blocks = (int)(((size_t)nlocal * 32 + 255) / 256);
+  if (fp64)
+    k_ell_from_csr<double4_32a><<<blocks, 256, 0, s>>>(nlocal, nall, x, types1, ntypes, offs, nbr,
+                                                       rc2, cap, nb_cnt, nb_jt, nb_vec, status);
+  else
+    k_ell_from_csr<float4><<<blocks, 256, 0, s>>>(nlocal, nall, x, types1, ntypes, offs, nbr, rc2,
+                                                  cap, nb_cnt, nb_jt, nb_vec, status);
+  return (int)cudaGetLastError();
+}
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types, const NbBuffers& nb,
                         int fp64, cudaStream_t s) {

@@ -190,6 +190,29 @@ int aenet_gpu_set_weights(const double* W);
  * layout it was read with). */
 int aenet_gpu_save_potential(int type_id, const char* filename);
 
+/* ---- caller's neighbour lists (MD engines) --------------------------------
+ * Energy and forces from the caller's full neighbour list, the interface an
+ * MD engine with its own domain decomposition (LAMMPS-style local + ghost
+ * atoms) needs: the engine keeps its neighbour lists, this evaluates the
+ * potential on the GPU.  HOST arrays:
+ *   x[3*nall]          positions of the nlocal local atoms, then the ghosts
+ *   type_ids[nall]     1-based type ids
+ *   neigh_offset[nlocal+1], neighbors[neigh_offset[nlocal]]
+ *                      CSR lists of each local atom's neighbours (indices
+ *                      into 0 .. nall-1, the atom itself excluded); pairs
+ *                      beyond Rc_max + 1e-3 are ignored, so lists built
+ *                      with a skin work as they are
+ * Outputs (may be NULL): *E_total (local atoms), E_atoms[nlocal],
+ * F[3*nall] forces on local AND ghost atoms (the engine adds the ghost
+ * forces to their owners), virial[9] of the local atoms' energy.
+ * Synchronous; returns an AENET status. */
+int aenet_gpu_neighbor_list_energy_forces(int nlocal, int nall, const double* x,
+                                          const int* type_ids,
+                                          const int* neigh_offset,
+                                          const int* neighbors, int precision,
+                                          double* E_total, double* E_atoms,
+                                          double* F, double* virial);
+
 /* ---- molecular dynamics -------------------------------------------------
  * Velocity-Verlet NVE dynamics of one periodic structure with the loaded
  * potentials, every step on the GPU (the integration ASE's VelocityVerlet
