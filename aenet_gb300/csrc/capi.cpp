@@ -2390,6 +2390,60 @@ EXPORT int aenet_gpu_neighbor_list_energy_forces(int nlocal, int nall, const dou
   return AENET_ERR_MALLOC;
 }
 
+// ---- training from stored descriptors (training-set files) -----------
+
+// Copy externally computed, normalised descriptors into the plan.
+EXPORT int aenet_gpu_plan_load_descriptors(aenet_gpu_plan* P, const double* G, int ld) {
+  if (!P || !G || !P->pd) return AENET_ERR_INPUT;
+  const int nsf_pad = P->pd->nsf_pad, N = P->natoms;
+  if (ld < P->pd->nsf_max || ld < 1) return AENET_ERR_INPUT;
+  const int cols = std::min(ld, nsf_pad);
+  if (P->fp64) {
+    std::vector<double> h((size_t)N * nsf_pad, 0.0);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < cols; ++k) h[(size_t)i * nsf_pad + k] = G[(size_t)i * ld + k];
+    if (cudaMemcpy(P->G, h.data(), 8 * h.size(), cudaMemcpyHostToDevice)) return AENET_ERR_CUDA;
+  } else {
+    std::vector<float> h((size_t)N * nsf_pad, 0.0f);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < cols; ++k) h[(size_t)i * nsf_pad + k] = (float)G[(size_t)i * ld + k];
+    if (cudaMemcpy(P->G, h.data(), 4 * h.size(), cudaMemcpyHostToDevice)) return AENET_ERR_CUDA;
+  }
+  return AENET_OK;
+}
+
+// The reference's energy loss and weight gradient from the loaded
+// descriptors (no positions, no neighbour search): networks, per-structure
+// energies, SSE = sum_s dE_s^2/2 and sum_s dE_s Dw_s.
+EXPORT int aenet_gpu_plan_descriptor_loss_gradient(aenet_gpu_plan* P, const int* d_types,
+                                                   const double* d_E_target, double* d_loss,
+                                                   double* d_grad, double* d_E, void* stream) {
+  if (!P || !d_types || !d_E_target || !d_loss || !d_grad) return AENET_ERR_INPUT;
+  const PotDevice& pd = *P->pd;
+  for (int t = 1; t < pd.ntypes; ++t)
+    if (std::fabs(pd.sp[t].E_scale - pd.sp[0].E_scale) > 1e-12 * std::fabs(pd.sp[0].E_scale))
+      return AENET_ERR_INPUT;
+  int st = plan_train_alloc(P);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (ck(ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s))) return AENET_ERR_CUDA;
+  DescBuffers d = desc_buffers(P, nullptr, false);
+  if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
+  if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->E_atom, P->e_part,
+                                         P->E_struct, s)))
+    return AENET_ERR_CUDA;
+  if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
+    return AENET_ERR_CUDA;
+  if (ck(ae_launch_loss(P->nstruc, P->geom_d, P->E_struct, d_E_target, P->Facc, nullptr, 0, 1.0, 0.0,
+                        pd.sp[0].E_scale, P->cE, P->U, P->loss_s, d_loss, P->fp64, s)) ||
+      ck(ae_launch_partition(P->natoms, pd.ntypes, P->types0, P->part_scratch, P->order,
+                             P->spec_off, s)) ||
+      ck(ae_launch_mlp_wgrad(pd, P->order, P->spec_off, P->G, nullptr, P->atom_struct, P->cE, 0.0, 0,
+                             P->partial, d_grad, P->fp64, s)))
+    return AENET_ERR_CUDA;
+  return AENET_OK;
+}
+
 // ---- network weights ------------------------------------------------
 
 EXPORT int aenet_gpu_network_nweights(int type_id) {

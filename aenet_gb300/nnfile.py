@@ -136,6 +136,24 @@ def _s(text, width):
     return _rec(b + b" " * (width - len(b)))
 
 
+def setup_payloads(stp, legacy=False):
+    """The Setup records of save_Setup (src/sfsetup.f90:585-609) as raw
+    payloads (no record framing), as potential and training-set files
+    store them."""
+    env = "".join("%-2s" % e for e in stp["envtypes"])
+    pay = lambda rec: rec[4:-4]
+    out = [_s(stp["description"], 1024), _s(stp["atomtype"], 2),
+           _i4([stp["nenv"]]), _rec(env.encode("latin-1")),
+           _f8([stp["Rc_min"]]), _f8([stp["Rc_max"]]), _s(stp["sftype"], 100),
+           _i4([stp["nsf"]]), _i4([stp["nsfparam"]]), _i4(stp["sf"]),
+           _f8(np.asarray(stp["sfparam"]).ravel()),
+           _i4(np.asarray(stp["sfenv"]).ravel()), _i4([stp.get("neval", 0)]),
+           _f8(stp["sfval_min"]), _f8(stp["sfval_max"]), _f8(stp["sfval_avg"])]
+    if not legacy:
+        out.append(_f8(stp["sfval_cov"]))
+    return [pay(r) for r in out]
+
+
 def write_nn(path, net, stp, ts, legacy=False):
     """Write a potential file.  ``ts`` needs keys scale, shift, typeName,
     E_atom (others default).  ``legacy=True`` omits ``sfval_cov``."""

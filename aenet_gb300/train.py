@@ -18,16 +18,33 @@ Two losses (``mode``):
                       dE_s = (E_t,s - E_s)/(E_scale N_s);
   LOSS_ENERGY_FORCES  w_E sum_s (E_s - E_t,s)^2/N_s^2 + w_F sum_i |F_i - F_t,i|^2.
 """
+import ctypes as C
+
 import numpy as np
 import torch
 
-from .core import FP64
-from .plan import LOSS_ENERGY, LOSS_ENERGY_FORCES, Plan
+from . import _lib
+from .core import FP64, check_status
+from .plan import LOSS_ENERGY, LOSS_ENERGY_FORCES, Plan, _p, _stream
 
-__all__ = ["Trainer", "LOSS_ENERGY", "LOSS_ENERGY_FORCES"]
+__all__ = ["Trainer", "DescriptorTrainer", "LOSS_ENERGY", "LOSS_ENERGY_FORCES"]
 
 
-class Trainer:
+class _Fit:
+    """L-BFGS-B over all weights (opt_bfgs_weights, src/optimize.f90:1721-1771)."""
+
+    def fit(self, maxiter=100, m=20, gtol=0.0, ftol=0.0, callback=None):
+        """Leaves the final weights loaded and returns scipy's OptimizeResult."""
+        from scipy.optimize import minimize
+        x0 = self.pot.get_weights()
+        res = minimize(self.loss_and_grad, x0, jac=True, method="L-BFGS-B", callback=callback,
+                       options={"maxcor": int(m), "maxiter": int(maxiter), "gtol": gtol,
+                                "ftol": ftol})
+        self.pot.set_weights(res.x)
+        return res
+
+
+class Trainer(_Fit):
     """Loss, gradient and L-BFGS-B fit of the loaded potentials on a fixed
     training set held in device memory.
 
@@ -73,16 +90,66 @@ class Trainer:
         self.evaluations += 1
         return float(self.loss.item()), self.grad.cpu().numpy().copy()
 
-    def fit(self, maxiter=100, m=20, gtol=0.0, ftol=0.0, callback=None):
-        """L-BFGS-B over all weights; leaves the best weights loaded and
-        returns scipy's OptimizeResult."""
-        from scipy.optimize import minimize
-        x0 = self.pot.get_weights()
-        res = minimize(self.loss_and_grad, x0, jac=True, method="L-BFGS-B", callback=callback,
-                       options={"maxcor": int(m), "maxiter": int(maxiter), "gtol": gtol,
-                                "ftol": ftol})
-        self.pot.set_weights(res.x)
-        return res
+    def close(self):
+        self.plan.close()
+
+
+class DescriptorTrainer(_Fit):
+    """train.x on a normalised training set (aenet training-set file): the
+    reference's energy loss and gradient (eval_next_structure,
+    src/train.f90:799-889) from the stored descriptors, on the GPU.
+
+    ``ts`` is a normalised :class:`aenet_gb300.trainset.TrainSet`; its
+    species names must be loaded in ``potentials``, whose energy scale and
+    shift are those of the training set (as train.x writes them)."""
+
+    def __init__(self, potentials, ts, precision=FP64):
+        from .nnfile import read_nn
+        if not ts.normalized:
+            raise ValueError("normalise the training set first (trainset.normalize)")
+        self.pot = potentials
+        lib = _lib.lib()
+        natoms = np.array([len(st["types"]) for st in ts.structures], dtype=np.int32)
+        N = int(natoms.sum())
+        ids = [potentials.get_type_id(n) for n in ts.type_names]
+        types = np.concatenate([np.array([ids[t - 1] for t in st["types"]], dtype=np.int32)
+                                for st in ts.structures])
+        ld = max(len(v) for st in ts.structures for v in st["sfval"])
+        G = np.zeros((N, ld))
+        row = 0
+        for st in ts.structures:
+            for v in st["sfval"]:
+                G[row, :len(v)] = v
+                row += 1
+        # totals in eV whose normalised cohesive part is the file's energy
+        sc, sh, ea = {}, {}, {}
+        for name in potentials.atom_types:
+            _, _, tsi, _ = read_nn(potentials.potential_files[name])
+            sc[name], sh[name] = 1.0 / tsi["scale"], tsi["shift"]
+            ea[name] = potentials.free_atom_energy(name)
+        names = potentials.atom_types
+        E_t = np.array([st["energy"] * sc[names[0]] + len(st["types"]) * sh[names[0]] +
+                        sum(ea[ts.type_names[t - 1]] for t in st["types"])
+                        for st in ts.structures])
+        self.plan = Plan(natoms, None, np.zeros(len(natoms), dtype=np.int32), precision=precision,
+                         coords0=np.zeros((N, 3)))
+        G = np.ascontiguousarray(G)
+        check_status(lib.aenet_gpu_plan_load_descriptors(self.plan._h,
+                                                         G.ctypes.data_as(C.c_void_p), ld))
+        dev = torch.device("cuda")
+        self.types = torch.as_tensor(types, device=dev).contiguous()
+        self.E_t = torch.as_tensor(E_t, device=dev).contiguous()
+        self.grad = torch.empty(potentials.nweights(), dtype=torch.float64, device=dev)
+        self.loss = torch.empty(1, dtype=torch.float64, device=dev)
+        self.E = torch.empty(len(natoms), dtype=torch.float64, device=dev)
+
+    def loss_and_grad(self, W=None):
+        if W is not None:
+            self.pot.set_weights(W)
+        check_status(_lib.lib().aenet_gpu_plan_descriptor_loss_gradient(
+            self.plan._h, _p(self.types), _p(self.E_t), _p(self.loss), _p(self.grad),
+            _p(self.E), _stream()))
+        return float(self.loss.item()), self.grad.cpu().numpy().copy()
 
     def close(self):
         self.plan.close()

@@ -177,6 +177,17 @@ int aenet_gpu_plan_loss_gradient(aenet_gpu_plan* plan, const double* d_coords,
                                  double w_F, double* d_loss, double* d_grad,
                                  double* d_E, double* d_F, void* stream);
 
+/* Training from stored descriptors (aenet training-set files hold the
+ * normalised descriptors of every atom, src/trainset.f90): load them into a
+ * plan (HOST G[N][ld], ld >= aenet_nsf_max, atom order of the plan), then
+ * evaluate the reference's energy loss and gradient from them
+ * (AENET_GPU_LOSS_ENERGY semantics; d_E_target are total energies in eV)
+ * without positions or a neighbour search. */
+int aenet_gpu_plan_load_descriptors(aenet_gpu_plan* plan, const double* G, int ld);
+int aenet_gpu_plan_descriptor_loss_gradient(aenet_gpu_plan* plan, const int* d_types,
+                                            const double* d_E_target, double* d_loss,
+                                            double* d_grad, double* d_E, void* stream);
+
 /* Network weights of all species, concatenated in type order, each the
  * reference's W(1:Wsize) (src/ext/feedforward.f90:55-89, the order
  * opt_bfgs_weights flattens them in, src/optimize.f90:1731-1737).

@@ -185,3 +185,50 @@ def test_lbfgs_fit_reduces_loss_and_saves_weights(cuda, batch, tmp_path):
         assert np.array_equal(net["W"], W[:ann.nweights(w.types[0])])
     finally:
         ann.release()
+
+
+def test_generate_and_train_from_trainset_file(cuda, oracle, batch, tmp_path):
+    """generate.x -> training-set file -> ts_normalize -> train.x energy
+    loss from the stored descriptors: raw descriptors match the oracle, and
+    the loss and gradient equal those of the positional path."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64
+    from aenet_gb300.generate import generate_trainset
+    from aenet_gb300.nnfile import read_nn
+    from aenet_gb300.trainset import normalize, read_trainset
+    from aenet_gb300.train import DescriptorTrainer, LOSS_ENERGY, Trainer
+    w, paths, tpaths = batch
+    E_t, F_t = _targets(w, tpaths)
+    structs = [{"positions": s.positions, "symbols": [w.types[t - 1] for t in s.types],
+                "cell": s.cell, "energy": E_t[k],
+                "name": "s%d" % k} for k, s in enumerate(w.structures)]
+    generate_trainset({t: paths[t] for t in w.types}, structs, str(tmp_path / "set.train"))
+    raw = read_trainset(str(tmp_path / "set.train"))
+    assert raw.setup_records is not None and len(raw.structures) == len(w.structures)
+    # raw descriptors of a few atoms against the oracle
+    oracle.load(w.types, paths)
+    s0 = w.structures[0]
+    _, centres, nb = oracle.neighbors(s0.cell, s0.positions, s0.types, atoms=[0, 1, 2])
+    for q in range(3):
+        nbcoo, _, _, nbt = nb[q]
+        ref = oracle.descriptor(centres[q], int(s0.types[q]), nbcoo, nbt, scaled=False)
+        assert np.abs(raw.structures[0]["sfval"][q] - ref).max() < 1e-10 * max(1, np.abs(ref).max())
+    # normalise with the potentials' own statistics and energy scale
+    stats = {}
+    for k, t in enumerate(w.types, start=1):
+        _, stp, tsi, _ = read_nn(paths[t])
+        sd = np.sqrt(np.asarray(stp["sfval_cov"]) - np.asarray(stp["sfval_avg"]) ** 2)
+        stats[k] = (np.asarray(stp["sfval_avg"]), np.where(sd <= 1e-10, 0.0, 1.0 / sd))
+    norm = normalize(raw, stats, scale=workloads.TS_SCALE, shift=workloads.TS_SHIFT)
+    ann = _ann(paths, w.types)
+    try:
+        dt = DescriptorTrainer(ann, norm, precision=FP64)
+        l1, g1 = dt.loss_and_grad()
+        dt.close()
+        tr = Trainer(ann, _structs(w), E_t, mode=LOSS_ENERGY, precision=FP64)
+        l0, g0 = tr.loss_and_grad()
+        tr.close()
+    finally:
+        ann.release()
+    assert abs(l1 - l0) <= 1e-9 * l0
+    assert np.abs(g1 - g0).max() <= 1e-9 * np.abs(g0).max()
