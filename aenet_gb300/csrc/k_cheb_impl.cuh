@@ -173,34 +173,6 @@ __device__ __forceinline__ void atomic_add3<double>(double* F, int atom, double 
   atomicAdd(F + 4 * atom + 2, fz);
 }
 
-// Block-local load balance: the 4 * GPW atoms of a block are ranked by
-// neighbour count (descending) in shared memory, so the GPW atoms sharing a
-// warp have similar loop lengths.  Results per atom do not depend on the
-// order.  Returns the atom of this group (>= natoms: none).
-template <int GPW>
-__device__ __forceinline__ int balanced_atom(const int* __restrict__ nb_cnt, int natoms, int slot) {
-  constexpr int ABLK = 4 * GPW;
-  __shared__ int s_key[ABLK], s_atom[ABLK];
-  const int blk0 = blockIdx.x * ABLK;
-  if (threadIdx.x < ABLK) {
-    const int a = blk0 + threadIdx.x;
-    s_key[threadIdx.x] = a < natoms ? nb_cnt[a] : -1;
-  }
-  __syncthreads();
-  if (threadIdx.x < ABLK) {
-    const int me = threadIdx.x, k = s_key[me];
-    int r = 0;
-#pragma unroll
-    for (int q = 0; q < ABLK; ++q) {
-      const int kq = s_key[q];
-      r += (kq > k) || (kq == k && q < me);
-    }
-    s_atom[r] = blk0 + me;
-  }
-  __syncthreads();
-  return s_atom[slot];
-}
-
 // ----------------------------------------------------------------------
 // forward
 // ----------------------------------------------------------------------
@@ -213,8 +185,8 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
   const int warp = threadIdx.x >> 5;
   const int grp = lane / LPA, sl = lane % LPA;
   const int wglobal = blockIdx.x * (blockDim.x >> 5) + warp;
-  const int gid = balanced_atom<GPW>(b.nb_cnt, b.natoms, warp * GPW + grp);
   if (wglobal * GPW >= b.natoms) return;   // whole warp idle
+  const int gid = wglobal * GPW + grp;
   const bool active = gid < b.natoms;
   const int i = active ? gid : b.natoms - 1;
   GroupSmem<T> sm = group_smem<T>(smem_raw, b.cap_a, pd.nsf_pad, warp * GPW + grp, false);
@@ -383,8 +355,8 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
   const int warp = threadIdx.x >> 5;
   const int grp = lane / LPA, sl = lane % LPA;
   const int wglobal = blockIdx.x * (blockDim.x >> 5) + warp;
-  const int gid = balanced_atom<GPW>(b.nb_cnt, b.natoms, warp * GPW + grp);
   if (wglobal * GPW >= b.natoms) return;
+  const int gid = wglobal * GPW + grp;
   const bool active = gid < b.natoms;
   const int i = active ? gid : b.natoms - 1;
   GroupSmem<T> sm = group_smem<T>(smem_raw, b.cap_a, pd.nsf_pad, warp * GPW + grp, true);
