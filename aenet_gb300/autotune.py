@@ -74,8 +74,22 @@ def tune(natoms, cells, pbc, positions, types, precision=core.MIXED, key=None, r
             results.append((_time(plan, p, t, reps), lp, cd, nk))
         plan.close()
         ms, lp, cd, nk = min(results)
-        best = {"neighbour_kernel": nk, "cell_div": cd, "lanes_per_atom": lp, "ms": ms,
-                "all": [[r[3], r[2], r[1], r[0]] for r in results]}
+        # the adjoint's lanes per atom, at the chosen forward shape
+        core.set_option("lanes_per_atom", lp)
+        plan = Plan(natoms, cells, pbc, precision=precision, coords0=positions)
+        adj = [(ms, 0)]
+        for la in lanes:
+            if la == lp:
+                continue
+            core.set_option("adjoint_lanes_per_atom", la)
+            adj.append((_time(plan, p, t, reps), la))
+        core.set_option("adjoint_lanes_per_atom", 0)
+        plan.close()
+        ms, la = min(adj)
+        best = {"neighbour_kernel": nk, "cell_div": cd, "lanes_per_atom": lp,
+                "adjoint_lanes_per_atom": la, "ms": ms,
+                "all": [[r[3], r[2], r[1], r[0]] for r in results] + [["adjoint", a[1], a[0]]
+                                                                      for a in adj[1:]]}
         if key and cache:
             os.makedirs(os.path.dirname(cache), exist_ok=True)
             entries[key] = best
@@ -84,5 +98,6 @@ def tune(natoms, cells, pbc, positions, types, precision=core.MIXED, key=None, r
             os.replace(tmp, cache)
     core.set_option("lanes_per_atom", best["lanes_per_atom"])
     core.set_option("cell_div", best["cell_div"])
-    core.set_option("neighbour_kernel", best.get("neighbour_kernel", "cell"))
+    core.set_option("neighbour_kernel", best.get("neighbour_kernel", "atom"))
+    core.set_option("adjoint_lanes_per_atom", best.get("adjoint_lanes_per_atom", 0))
     return best

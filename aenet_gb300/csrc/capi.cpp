@@ -267,6 +267,7 @@ struct State {
   int angular_legacy = 0;
   int cell_div = 2;
   int lpa_default = 16;
+  int lpa_adjoint = 0;        // lanes per atom of the adjoint (0: as the forward)
   int networks_tc = 1;       // tensor-core networks on the mixed path when eligible
   int nb_cell = 0;           // neighbour search: one warp per home cell (1) or per atom (0)
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
@@ -1201,6 +1202,7 @@ int plan_adjoint(aenet_gpu_plan* P, const double* grad_scale, double* d_out, dou
   if (cudaMemsetAsync(P->Facc, 0, 4 * tsz * (size_t)P->natoms, s)) return AENET_ERR_CUDA;
   if (d_virial && cudaMemsetAsync(P->virial, 0, 72 * (size_t)P->nstruc, s)) return AENET_ERR_CUDA;
   DescBuffers d = desc_buffers(P, grad_scale, d_virial != nullptr);
+  if (g.lpa_adjoint) d.lpa = g.lpa_adjoint;
   int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, P->fp64, s)
                                              : ae_launch_chebyshev_adjoint(pd, d, P->fp64, s);
   if (ck(e)) return AENET_ERR_CUDA;
@@ -1818,6 +1820,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     g.dev_ready = false;
     return AENET_OK;
   }
+  if (k == "adjoint_lanes_per_atom") {
+    int d = atoi(v.c_str());
+    if (d != 0 && d != 8 && d != 16 && d != 32) return AENET_ERR_INPUT;
+    g.lpa_adjoint = d;
+    return AENET_OK;
+  }
   if (k == "lanes_per_atom") {
     int d = atoi(v.c_str());
     if (d != 8 && d != 16 && d != 32) return AENET_ERR_INPUT;
@@ -2366,6 +2374,7 @@ EXPORT int aenet_gpu_neighbor_list_energy_forces(int nlocal, int nall, const dou
       return AENET_ERR_CUDA;
     DescBuffers d = desc_buffers(P, nullptr, true);
     d.F = c.Facc;
+    if (g.lpa_adjoint) d.lpa = g.lpa_adjoint;
     int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, P->fp64, s)
                                                : ae_launch_chebyshev_adjoint(pd, d, P->fp64, s);
     if (ck(e) || ck(ae_launch_forces_out(nall, c.Facc, P->fp64, c.F, 1.0, s))) return AENET_ERR_CUDA;
@@ -2544,6 +2553,7 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   cudaEventRecord(ev[5], s);
   const size_t tsz = P->fp64 ? 8 : 4;
   cudaMemsetAsync(P->Facc, 0, 4 * tsz * (size_t)P->natoms, s);
+  if (g.lpa_adjoint) d.lpa = g.lpa_adjoint;
   e |= (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, P->fp64, s)
                                           : ae_launch_chebyshev_adjoint(pd, d, P->fp64, s);
   cudaEventRecord(ev[6], s);

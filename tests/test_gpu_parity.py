@@ -486,3 +486,42 @@ def test_tensor_core_networks_match_simt_and_fp64(cuda, oracle, aucu, tmp_path, 
     assert dE.max() < 1e-4
     dF = out["tensor"]["forces"] - out["simt"]["forces"]
     assert np.sqrt((dF ** 2).mean()) < 1e-3
+
+
+def test_k5_rotation_invariance_and_fcc_shell_on_gpu(cuda, cu256):
+    """K-5 on the GPU: energies invariant under a rotation of structure and
+    cell (FP64 1e-10 eV/atom, mixed 1e-5 eV/atom), forces rotate with it,
+    and every atom of a perfect FCC crystal has 12 neighbours in its first
+    shell."""
+    torch = cuda
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED
+    from aenet_gb300.plan import Plan
+    w, paths = cu256
+    s = w.structures[0]
+    rng = np.random.default_rng(11)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    ann = _ann(paths, w.types)
+    try:
+        for prec, tol in ((FP64, 1e-10), (MIXED, 1e-5)):
+            r0 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=prec)
+            r1 = ann.structure_energy_forces(s.positions @ q, s.types, s.cell @ q, precision=prec)
+            assert abs(r1["energy"] - r0["energy"]) / s.natoms < tol
+            ftol = 1e-9 if prec == FP64 else 1e-3
+            assert np.abs(r1["forces"] - r0["forces"] @ q).max() < ftol
+        pos, cell = workloads.fcc_positions(4, 3.61)
+        plan = Plan([len(pos)], cell[None], precision=FP64)
+        p = torch.tensor(pos, device="cuda")
+        t = torch.ones(len(pos), dtype=torch.int32, device="cuda")
+        plan.run(p, t)
+        plan.check()
+        _, cnt, _, vec = plan.neighbors()
+        d = vec[..., 3].cpu().numpy()
+        c = cnt.cpu().numpy()
+        first = [(d[i, :c[i]] < 3.61 / np.sqrt(2) + 0.05).sum() for i in range(len(pos))]
+        assert set(first) == {12}
+        plan.close()
+    finally:
+        ann.release()

@@ -159,3 +159,25 @@ def test_oracle_weight_gradient_matches_finite_differences(oracle, k1, tmp_path)
             f[m] = energy(w)
         fd = (8 * (f[1] - f[-1]) - (f[2] - f[-2])) / (12 * h)
         assert abs(fd - g[k]) <= 1e-7 * max(1.0, abs(g[k])), (k, fd, g[k])
+
+
+def test_k5_fcc_neighbour_count_and_rotation_invariance(oracle, tmp_path):
+    """K-5 (src/tests/*.f90 properties): 12 nearest neighbours in FCC, and
+    energies invariant under a rotation of the structure with its cell."""
+    from aenet_gb300 import workloads
+    from tests import helpers
+    w = workloads.cu_fcc_256()
+    paths = helpers.make_potentials(oracle, w, str(tmp_path), max_atoms=64)
+    oracle.load(w.types, paths)
+    pos, cell = workloads.fcc_positions(4, 3.61)
+    types = np.ones(len(pos), dtype=np.int32)
+    _, _, nb = oracle.neighbors(cell, pos, types, Rc=3.61 / np.sqrt(2) + 0.05, atoms=[0, 17, 100])
+    assert [len(x[0]) for x in nb] == [12, 12, 12]
+    s = w.structures[0]
+    rng = np.random.default_rng(11)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    e0 = oracle.structure(s.cell, s.positions, s.types, forces=False)[1]
+    e1 = oracle.structure(s.cell @ q, s.positions @ q, s.types, forces=False)[1]
+    assert abs(e1 - e0) / s.natoms < 1e-10
