@@ -203,7 +203,7 @@ struct VecOut<double4_32a> {
 };
 
 template <typename T4>
-__global__ void __launch_bounds__(256) k_neighbors(int natoms, NbBuffers nb) {
+__global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) {
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= natoms) return;
