@@ -371,7 +371,7 @@ def run_gb300(args):
               "neighbours": 24 + nb["n_r"] * 20 + 16 * 27}
     dom_ms = stages[dom]
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic_per_atom.json")
+    tf = os.path.join(ROOT, "profiles", "traffic_per_atom.txt")
     if os.path.exists(tf):
         per_atom = json.load(open(tf)).get(kernels[dom])
         traffic = None if per_atom is None else per_atom * N
