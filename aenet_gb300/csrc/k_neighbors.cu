@@ -204,6 +204,10 @@ struct VecOut<double4_32a> {
 
 template <typename T4>
 __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) {
+  __shared__ int su_base[8][32];      // per warp: cell_atoms offset of each unit
+  __shared__ float4 su_sh[8][32];     // image shift and packed image of each unit
+  __shared__ int su_first[8][32];     // unit starting at each offset of a batch
+  const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= natoms) return;
@@ -297,31 +301,37 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
       if (lane >= d) incl += w;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
+    // unit table of this round in shared memory: candidate q belongs to the
+    // unit whose start is the last start <= q
+    const int start = incl - len;
+    __syncwarp();   // the previous round's readers are done
+    su_base[warp][lane] = beg - start;   // cell_atoms index = base + q
+    su_sh[warp][lane] = make_float4(sh0, sh1, sh2,
+                                    __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) |
+                                                   ((T2 & 1023) << 20)));
+    __syncwarp();
+    int carry = 0;
     for (int qb = 0; qb < total; qb += 32) {
       const int q = qb + lane;
-      // owner unit: first lane whose inclusive prefix exceeds q
-      int lo = 0, hi = 31;
-#pragma unroll
-      for (int step = 0; step < 5; ++step) {
-        const int mid = (lo + hi) >> 1;
-        const int pv = __shfl_sync(0xffffffffu, incl, mid);
-        if (pv > q) hi = mid; else lo = mid + 1;
-      }
-      const int own = lo;
-      const int own_incl = __shfl_sync(0xffffffffu, incl, own);
-      const int own_len = __shfl_sync(0xffffffffu, len, own);
-      const int own_beg = __shfl_sync(0xffffffffu, beg, own);
-      const int oT0 = __shfl_sync(0xffffffffu, T0, own);
-      const int oT1 = __shfl_sync(0xffffffffu, T1, own);
-      const int oT2 = __shfl_sync(0xffffffffu, T2, own);
-      const float osh0 = __shfl_sync(0xffffffffu, sh0, own);
-      const float osh1 = __shfl_sync(0xffffffffu, sh1, own);
-      const float osh2 = __shfl_sync(0xffffffffu, sh2, own);
+      // units starting inside this batch mark their offsets
+      const bool starts = len > 0 && start >= qb && start < qb + 32;
+      __syncwarp();   // the previous batch's readers are done
+      if (starts) su_first[warp][start - qb] = lane;
+      const unsigned marks = __reduce_or_sync(0xffffffffu, starts ? (1u << (start - qb)) : 0u);
+      __syncwarp();
+      const unsigned upto = marks & (0xffffffffu >> (31 - lane));
+      const int own = upto ? su_first[warp][31 - __clz(upto)] : carry;
+      carry = __shfl_sync(0xffffffffu, own, 31);
+      const float4 osh = su_sh[warp][own];
+      const int img = __float_as_int(osh.w);
+      const int oT0 = sext10i(img & 1023), oT1 = sext10i((img >> 10) & 1023),
+                oT2 = sext10i((img >> 20) & 1023);
+      const float osh0 = osh.x, osh1 = osh.y, osh2 = osh.z;
       bool accept = false;
       int j = -1, tj = 0;
       float dx = 0.f, dy = 0.f, dz = 0.f, dd2 = 0.f;
       if (q < total) {
-        const int p = own_beg + (q - (own_incl - own_len));
+        const int p = su_base[warp][own] + q;
         const float4 rj = nb.cell_pos[p];
         j = nb.cell_atoms[p];
         tj = __float_as_int(rj.w);

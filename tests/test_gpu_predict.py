@@ -56,3 +56,29 @@ def test_predict_driver_cu_dimer_report(cuda, tmp_path):
             F = np.array([float(x) for x in rows[2 * n + a][3:]])
             assert np.abs(F - k3["forces"][q][a]).max() <= 1.01e-6
     assert "The maximum force is acting on atom" in text
+
+
+def test_predict_driver_relaxation_lowers_energy(cuda, oracle, tmp_path):
+    """RELAX through the driver: a perturbed 256-atom Cu cell relaxes to a
+    lower cohesive energy and a smaller RMS force, and the report shows the
+    optimised coordinates."""
+    from aenet_gb300 import predict, workloads
+    from aenet_gb300.xsf import write_xsf
+    from tests import helpers
+    w = workloads.cu_fcc_256()
+    paths = helpers.make_potentials(oracle, w, str(tmp_path), max_atoms=64)
+    s = w.structures[0]
+    write_xsf(str(tmp_path / "cu.xsf"), ["Cu"] * s.natoms, s.positions, cell=s.cell)
+    inp = tmp_path / "predict.in"
+    inp.write_text("TYPES\n1\nCu\n\nNETWORKS\nCu %s\n\nRELAX\nmethod=bfgs F_conv=1.0d-3 "
+                   "E_conv=1.0d-9 steps=30\n\nFILES\n1\n%s\n" % (paths["Cu"], tmp_path / "cu.xsf"))
+    out = io.StringIO()
+    assert predict.main([str(inp)], out=out) == 0
+    text = out.getvalue()
+    assert "Geometry optimization:" in text and "(optimized)" in text
+    rows = re.findall(r"^\s+(\d+)\s+(-?\d+\.\d+)\s+(\d+\.\d+)", text, re.M)
+    dE = [float(r[1]) for r in rows]
+    rms = [float(r[2]) for r in rows]
+    assert len(rows) >= 2 and dE[-1] < 0.0 and rms[-1] < rms[0]
+    final_rms = float(re.findall(r"RMS force\s+:\s+(\S+)", text)[-1])
+    assert final_rms < rms[0]
