@@ -433,6 +433,9 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
   __shared__ float4 s_pos[NBC_WARPS][32];     // candidate position, species bits in w
   __shared__ float4 s_shift[NBC_WARPS][32];   // image shift, packed image in w
   __shared__ int s_j[NBC_WARPS][32];
+  __shared__ int su_base[NBC_WARPS][32];
+  __shared__ float4 su_sh[NBC_WARPS][32];
+  __shared__ int su_first[NBC_WARPS][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gc = blockIdx.x * NBC_WARPS + warp;
   if (gc >= ncells) return;
@@ -523,33 +526,31 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
         if (lane >= d) incl += w;
       }
       const int total = __shfl_sync(0xffffffffu, incl, 31);
+      // unit table of this round (see k_neighbors)
+      const int start = incl - len;
+      __syncwarp();
+      su_base[warp][lane] = beg - start;
+      su_sh[warp][lane] = make_float4(sh0, sh1, sh2,
+                                      __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) |
+                                                     ((T2 & 1023) << 20)));
+      __syncwarp();
+      int carry = 0;
       for (int qb = 0; qb < total; qb += 32) {
         // ---- stage 32 candidates
         const int q = qb + lane;
-        int lo2 = 0, hi2 = 31;
-#pragma unroll
-        for (int step = 0; step < 5; ++step) {
-          const int mid = (lo2 + hi2) >> 1;
-          const int pv = __shfl_sync(0xffffffffu, incl, mid);
-          if (pv > q) hi2 = mid; else lo2 = mid + 1;
-        }
-        const int own = lo2;
-        const int own_incl = __shfl_sync(0xffffffffu, incl, own);
-        const int own_len = __shfl_sync(0xffffffffu, len, own);
-        const int own_beg = __shfl_sync(0xffffffffu, beg, own);
-        const int oT0 = __shfl_sync(0xffffffffu, T0, own);
-        const int oT1 = __shfl_sync(0xffffffffu, T1, own);
-        const int oT2 = __shfl_sync(0xffffffffu, T2, own);
-        const float osh0 = __shfl_sync(0xffffffffu, sh0, own);
-        const float osh1 = __shfl_sync(0xffffffffu, sh1, own);
-        const float osh2 = __shfl_sync(0xffffffffu, sh2, own);
+        const bool starts = len > 0 && start >= qb && start < qb + 32;
+        __syncwarp();   // readers of the previous batch are done
+        if (starts) su_first[warp][start - qb] = lane;
+        const unsigned marks = __reduce_or_sync(0xffffffffu, starts ? (1u << (start - qb)) : 0u);
+        __syncwarp();
+        const unsigned upto = marks & (0xffffffffu >> (31 - lane));
+        const int own = upto ? su_first[warp][31 - __clz(upto)] : carry;
+        carry = __shfl_sync(0xffffffffu, own, 31);
         if (q < total) {
-          const int p = own_beg + (q - (own_incl - own_len));
+          const int p = su_base[warp][own] + q;
           s_pos[warp][lane] = nb.cell_pos[p];
           s_j[warp][lane] = nb.cell_atoms[p];
-          s_shift[warp][lane] = make_float4(
-              osh0, osh1, osh2,
-              __int_as_float((oT0 & 1023) | ((oT1 & 1023) << 10) | ((oT2 & 1023) << 20)));
+          s_shift[warp][lane] = su_sh[warp][own];
         }
         __syncwarp();
         // ---- test them against this lane's home atom
