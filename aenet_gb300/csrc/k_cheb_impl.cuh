@@ -297,34 +297,46 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
     ang[q] = T(0);
     angs[q] = T(0);
   }
-  const int P = na * (na - 1) / 2;
-  const int Ploop = warp_max(P);
-  PairWalk pw;
-  pw.start(sl, na);
-  for (int p = sl; p < Ploop; p += LPA) {
-    if (p < P) {
-      const T4 uj = sm.au[pw.a], uk = sm.au[pw.b];
-      const T4 fj = sm.af[pw.a], fk = sm.af[pw.b];
-      const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
-      const T w = fj.x * fk.x;
-      const T sw = fj.z * fk.z * w;
-      T x, dxdc;
-      angular_arg(cosv, ct.angular_legacy, x, dxdc);
-      const T x2 = x + x;
-      T tm1 = T(1), t0 = x;
-      ang[0] += w;
-      angs[0] += sw;
+  // pairs (a, k = a + t mod na), t = 1 .. na/2, as in the adjoint: the
+  // owner of a keeps it in registers and every pair is visited once
+  const int tmax = na / 2;
+  for (int a0 = 0; a0 < na; a0 += LPA) {
+    const int a = a0 + sl;
+    const bool own = active && a < na;
+    T4 uj, fj;
+    if (own) {
+      uj = sm.au[a];
+      fj = sm.af[a];
+    } else {
+      uj.x = uj.y = uj.z = uj.w = T(0);
+      fj.x = fj.y = fj.z = fj.w = T(0);
+    }
+    for (int t = 1; t <= tmax; ++t) {
+      int k = a + t;
+      if (k >= na) k -= na;
+      if (own && !(2 * t == na && a >= tmax)) {
+        const T4 uk = sm.au[k];
+        const T4 fk = sm.af[k];
+        const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
+        const T w = fj.x * fk.x;
+        const T sw = fj.z * fk.z * w;
+        T x, dxdc;
+        angular_arg(cosv, ct.angular_legacy, x, dxdc);
+        const T x2 = x + x;
+        T tm1 = T(1), t0 = x;
+        ang[0] += w;
+        angs[0] += sw;
 #pragma unroll
-      for (int q = 1; q < A; ++q) {
-        if (!GUARD || q < aN) {
-          ang[q] = fma(w, t0, ang[q]);
-          angs[q] = fma(sw, t0, angs[q]);
-          const T tn = fma(x2, t0, -tm1);
-          tm1 = t0;
-          t0 = tn;
+        for (int q = 1; q < A; ++q) {
+          if (!GUARD || q < aN) {
+            ang[q] = fma(w, t0, ang[q]);
+            angs[q] = fma(sw, t0, angs[q]);
+            const T tn = fma(x2, t0, -tm1);
+            tm1 = t0;
+            t0 = tn;
+          }
         }
       }
-      pw.advance(na, LPA);
     }
   }
 #pragma unroll
