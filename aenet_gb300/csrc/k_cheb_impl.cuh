@@ -446,9 +446,6 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
     // grad_j E = c R_ij / d; the force on j is minus that
     const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? c / d : T(0);
     const T gx = inv * v.x, gy = inv * v.y, gz = inv * v.z;
-    fix += gx;
-    fiy += gy;
-    fiz += gz;
     const bool inA = d <= a_Rc && d >= T(SFB_EPS);
     const unsigned m = __ballot_sync(0xffffffffu, inA) & gmask;
     bool staged = false;
@@ -462,7 +459,7 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
         u.x = v.x * invd;
         u.y = v.y * invd;
         u.z = v.z * invd;
-        u.w = d;
+        u.w = invd;   // the angular loop needs 1/d only
         f.x = fc;
         f.y = dfc;
         f.z = s;
@@ -474,6 +471,12 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
         sm.fbuf[3 * k + 2] = -gz;
         staged = true;
       }
+    }
+    if (!staged) {
+      // staged neighbours hand their force to the central atom at the end
+      fix += gx;
+      fiy += gy;
+      fiz += gz;
     }
     if (valid && !staged && c != T(0)) {
       atomic_add3<T>(F, jatom, -gx, -gy, -gz);
@@ -519,7 +522,7 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
       ua.w = T(1);
       fa.x = fa.y = fa.z = fa.w = T(0);
     }
-    const T inva = T(1) / ua.w;
+    const T inva = ua.w;
     T gax = T(0), gay = T(0), gaz = T(0);
     for (int t = 1; t <= tmax; ++t) {
       int k = a + t;
@@ -549,7 +552,7 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
             u0 = un;
           }
         }
-        const T invk = T(1) / uk.w;
+        const T invk = uk.w;
         const T Bc = w * Bv * dxdc;
         const T dEda = fa.y * fk.x * Av, ca = Bc * inva;   // d/dd_a of w A, (dE/dcos)/d_a
         const T dEdk = fa.x * fk.y * Av, ck = Bc * invk;
@@ -565,9 +568,6 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
         sm.fbuf[3 * k] -= hx;
         sm.fbuf[3 * k + 1] -= hy;
         sm.fbuf[3 * k + 2] -= hz;
-        fix += gx + hx;
-        fiy += gy + hy;
-        fiz += gz + hz;
       }
       __syncwarp(gmask);
     }
@@ -584,6 +584,9 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
     const int slot = (int)sm.af[a].w;
     const T fx = sm.fbuf[3 * a], fy = sm.fbuf[3 * a + 1], fz = sm.fbuf[3 * a + 2];
     atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
+    fix -= fx;   // the central atom takes minus the neighbour's force
+    fiy -= fy;
+    fiz -= fz;
     if (want_virial) {
       const T4 v = vec[slot];
       w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
