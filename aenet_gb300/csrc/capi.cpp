@@ -270,6 +270,7 @@ struct State {
   int lpa_adjoint = 0;        // lanes per atom of the adjoint (0: as the forward)
   int networks_tc = 1;       // tensor-core networks on the mixed path when eligible
   int nb_cell = 0;           // neighbour search: one warp per home cell (1) or per atom (0)
+  int angular_moments = 1;   // FP32 angular terms in moment form where instantiated
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
@@ -312,6 +313,46 @@ float typespin(int num_types, int l) {
     s = s + 1;
   }
   return 0.f;
+}
+
+// Legendre expansion of the angular basis: T_n(x(c)) = sum_l q[n][l] P_l(c)
+// for n < a_N <= AE_MOMA, x(c) = c or the legacy (2c - pi)/pi of
+// sfbasis.f90's PI.  Monomial coefficients in c, peeled from the top degree.
+std::vector<float> legendre_table(int a_N, int legacy) {
+  const int D = AE_MOMA;
+  std::vector<float> q(D * D, 0.f);
+  if (a_N > D) return q;
+  const double pi = 3.14159265358979;
+  const double al = legacy ? 2.0 / pi : 1.0, be = legacy ? -1.0 : 0.0;
+  std::vector<std::vector<double>> Tn(D, std::vector<double>(D, 0.0)), Pl = Tn;
+  Tn[0][0] = 1.0;
+  if (D > 1) {
+    Tn[1][0] = be;
+    Tn[1][1] = al;
+  }
+  for (int k = 1; k + 1 < D; ++k)
+    for (int e = 0; e < D; ++e) {
+      double v = 2.0 * be * Tn[k][e] - Tn[k - 1][e];
+      if (e > 0) v += 2.0 * al * Tn[k][e - 1];
+      Tn[k + 1][e] = v;
+    }
+  Pl[0][0] = 1.0;
+  if (D > 1) Pl[1][1] = 1.0;
+  for (int k = 1; k + 1 < D; ++k)
+    for (int e = 0; e < D; ++e) {
+      double v = -k * Pl[k - 1][e];
+      if (e > 0) v += (2.0 * k + 1.0) * Pl[k][e - 1];
+      Pl[k + 1][e] = v / (k + 1.0);
+    }
+  for (int n = 0; n < a_N; ++n) {
+    std::vector<double> rem = Tn[n];
+    for (int l = n; l >= 0; --l) {
+      const double c = rem[l] / Pl[l][l];
+      q[n * D + l] = (float)c;
+      for (int e = 0; e <= l; ++e) rem[e] -= c * Pl[l][e];
+    }
+  }
+  return q;
 }
 
 int local_type(const HostSetup& s, const std::string& name) {
@@ -534,6 +575,13 @@ int build_device_tables() {
   }
   // split-BF16 images for the tensor-core networks
   std::vector<unsigned char> tc_img = make_tc_image(pd, scale);
+  // Legendre tables of the moment form (Chebyshev species)
+  std::vector<float> qleg((size_t)g.ntypes * AE_MOMA * AE_MOMA, 0.f);
+  for (int t = 0; t < g.ntypes; ++t)
+    if (pd.sp[t].sftype == AE_SF_CHEBYSHEV) {
+      std::vector<float> qt = legendre_table(pd.sp[t].cheb.a_N, pd.sp[t].cheb.angular_legacy);
+      std::copy(qt.begin(), qt.end(), qleg.begin() + (size_t)t * AE_MOMA * AE_MOMA);
+    }
   g.scale_host = scale;
   // Behler tables
   std::vector<std::vector<unsigned char>> bt;
@@ -558,6 +606,8 @@ int build_device_tables() {
   blob_bytes = align(blob_bytes + scale32.size() * 4);
   size_t off_tc = blob_bytes;
   blob_bytes = align(blob_bytes + tc_img.size());
+  size_t off_q = blob_bytes;
+  blob_bytes = align(blob_bytes + qleg.size() * 4);
   size_t off_beh = blob_bytes;
   std::vector<size_t> beh_off;
   for (auto& b : bt) {
@@ -576,6 +626,7 @@ int build_device_tables() {
   for (size_t q = 0; q < bt.size(); ++q)
     cudaMemcpy(base + off_beh + beh_off[q], bt[q].data(), bt[q].size(), cudaMemcpyHostToDevice);
   if (!tc_img.empty()) cudaMemcpy(base + off_tc, tc_img.data(), tc_img.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(base + off_q, qleg.data(), qleg.size() * 4, cudaMemcpyHostToDevice);
   if (cudaDeviceSynchronize() != cudaSuccess) return AENET_ERR_CUDA;
   pd.shift = (const double*)(base + off_shift);
   pd.scale = (const double*)(base + off_scale);
@@ -585,6 +636,7 @@ int build_device_tables() {
   pd.scale32 = (const float*)(base + off_sc32);
   pd.behler_blob = (const unsigned char*)(base + off_beh);
   pd.tc_img = tc_img.empty() ? nullptr : (const unsigned char*)(base + off_tc);
+  pd.qleg = (const float*)(base + off_q);
   for (size_t q = 0; q < bt.size(); ++q) pd.sp[q].behler_off = (int)beh_off[q];
   g.pd = pd;
   g.blob = std::move(blob);
@@ -787,6 +839,8 @@ struct aenet_gpu_plan {
   int* nb_jt = nullptr;
   void* nb_vec = nullptr;
   int* nb_img = nullptr;
+  float* M = nullptr;         // angular moments of the FP32 moment form
+  int mom_pad = 0;
   void* G = nullptr;
   void* dEdG = nullptr;
   double* E_atom = nullptr;
@@ -1019,6 +1073,14 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_jt = take(4 * npairs);
   size_t o_vec = take((P->fp64 ? 32 : 16) * npairs);
   size_t o_img = P->keep_images ? take(4 * npairs) : 0;
+  // moment buffer of the FP32 path: both blocks' moments per atom
+  P->mom_pad = 0;
+  if (!P->fp64 && P->pd && P->pd->qleg) {
+    int aN = 0;
+    for (int t = 0; t < P->pd->ntypes; ++t) aN = std::max(aN, P->pd->sp[t].cheb.a_N);
+    if (aN <= AE_MOMA) P->mom_pad = (2 * aN * aN + 3) & ~3;
+  }
+  size_t o_M = P->mom_pad ? take(4 * (size_t)P->mom_pad * N) : 0;
   size_t o_G = take(tsz * nsf_pad * N);
   size_t o_dG = take(tsz * nsf_pad * N);
   size_t o_E = take(8 * (size_t)N);
@@ -1050,6 +1112,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->nb_jt = (int*)(b + o_jt);
   P->nb_vec = (void*)(b + o_vec);
   P->nb_img = P->keep_images ? (int*)(b + o_img) : nullptr;
+  P->M = P->mom_pad ? (float*)(b + o_M) : nullptr;
   P->G = (void*)(b + o_G);
   P->dEdG = (void*)(b + o_dG);
   P->E_atom = (double*)(b + o_E);
@@ -1120,6 +1183,10 @@ DescBuffers desc_buffers(aenet_gpu_plan* P, const double* grad_scale, bool viria
   d.atom_struct = P->atom_struct;
   d.grad_scale = grad_scale;
   d.status = P->status;
+  if (g.angular_moments && P->M) {
+    d.M = P->M;
+    d.mom_pad = P->mom_pad;
+  }
   return d;
 }
 
@@ -1841,6 +1908,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
   if (k == "neighbour_kernel") {
     if (v == "cell") g.nb_cell = 1;
     else if (v == "atom") g.nb_cell = 0;
+    else return AENET_ERR_INPUT;
+    return AENET_OK;
+  }
+  if (k == "angular_terms") {
+    if (v == "moments") g.angular_moments = 1;
+    else if (v == "pairs") g.angular_moments = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;
   }

@@ -27,6 +27,7 @@
 #define AE_INDEX_MASK ((1 << AE_TYPE_SHIFT) - 1)
 #define AE_MAXG4 64          // Behler angular functions per triple type
 #define AE_MAXG2 64          // Behler radial functions per pair type
+#define AE_MOMA 7            // angular functions (order + 1) of the moment form
 
 // status bits written by kernels into a device word
 #define AE_ST_NB_OVERFLOW 1u
@@ -111,6 +112,10 @@ struct PotDevice {
   int tc_kin, tc_h;                   // padded input and hidden widths (32 or 64)
   int tc_tanh;                        // every species: tanh hidden layers, linear output
   const unsigned char* tc_img;        // [ntypes][TcLayout::bytes]
+  // angular terms in moment form (FP32 path): per species the Legendre
+  // expansion T_n(x(c)) = sum_l q[n][l] P_l(c) of the angular basis in
+  // c = cos(theta), [ntypes][AE_MOMA][AE_MOMA]; null when unavailable
+  const float* qleg;
 };
 
 // Per-species image for the tensor-core networks.  Operand tiles are
@@ -229,6 +234,8 @@ struct DescBuffers {
   unsigned* status;
   const void* U;               // [N] T4 per-atom directions of the tangent pass
   void* V;                     // [N][nsf_pad] (T) normalised descriptor tangents
+  float* M;                    // [N][mom_pad] angular moments (FP32 moment form) or null
+  int mom_pad;
 };
 
 int ae_launch_chebyshev_forward(const PotDevice& pd, const DescBuffers& b,

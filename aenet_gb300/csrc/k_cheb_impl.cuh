@@ -31,6 +31,7 @@
 // memory once; the central atom receives minus the sum.
 #pragma once
 #include "common.h"
+#include "k_cheb_mom.cuh"
 
 namespace cheb {
 
@@ -118,24 +119,44 @@ struct GroupSmem {
   T* g;                         // [nsf_pad] dE/dG
 };
 
+// the staging area of the forward doubles as the moment reduction scratch
+// (`scratch` bytes at least)
 template <typename T>
-__host__ __device__ inline size_t group_smem_bytes(int cap_a, int nsf_pad, bool adjoint) {
+__host__ __device__ inline size_t group_smem_bytes(int cap_a, int nsf_pad, bool adjoint,
+                                                   size_t scratch = 0) {
   using T4 = typename Vec4<T>::type;
-  size_t per = 2 * sizeof(T4) * cap_a + (adjoint ? (3 * sizeof(T) * cap_a + sizeof(T) * nsf_pad) : 0);
+  size_t stage = 2 * sizeof(T4) * cap_a;
+  if (stage < scratch) stage = scratch;
+  size_t per = stage + (adjoint ? (3 * sizeof(T) * cap_a + sizeof(T) * nsf_pad) : 0);
   return (per + 31) & ~size_t(31);
 }
 
 template <typename T>
 __device__ __forceinline__ GroupSmem<T> group_smem(unsigned char* base, int cap_a, int nsf_pad,
-                                                   int group, bool adjoint) {
+                                                   int group, bool adjoint, size_t scratch = 0) {
   using T4 = typename Vec4<T>::type;
-  unsigned char* p = base + group_smem_bytes<T>(cap_a, nsf_pad, adjoint) * group;
+  unsigned char* p = base + group_smem_bytes<T>(cap_a, nsf_pad, adjoint, scratch) * group;
   GroupSmem<T> w;
   w.au = reinterpret_cast<T4*>(p);
   w.af = w.au + cap_a;
   w.fbuf = reinterpret_cast<T*>(w.af + cap_a);
   w.g = w.fbuf + 3 * cap_a;
   return w;
+}
+
+// moment form: values per lane in the reduction (both blocks' moments, then
+// the two weight sums), padded to whole float4
+template <int A>
+__host__ __device__ constexpr int mom_nv() {
+  return 2 * A * A + 2;
+}
+template <int A>
+__host__ __device__ constexpr int mom_nvp() {
+  return (mom_nv<A>() + 3) & ~3;
+}
+template <int A, int LPA>
+__host__ __device__ constexpr size_t mom_scratch_bytes() {
+  return sizeof(float) * (size_t)(LPA + 1) * mom_nvp<A>();
 }
 
 // row-major walk of the upper triangle a < b < na with a fixed stride
@@ -173,10 +194,97 @@ __device__ __forceinline__ void atomic_add3<double>(double* F, int atom, double 
   atomicAdd(F + 4 * atom + 2, fz);
 }
 
+// Angular block of the forward in moment form (FP32): the group's lanes
+// accumulate moments over the staged neighbours, the partial sums are
+// reduced through the (then free) staging area, the moments are stored for
+// the adjoint and each output lane assembles its G_n from the power spectra.
+template <int A, int LPA>
+__device__ __forceinline__ void forward_moments(const PotDevice& pd, const DescBuffers& b,
+                                                const GroupSmem<float>& sm, const ChebTable& ct,
+                                                int na, int sl, unsigned gmask, bool active, int i,
+                                                int ti, bool multi, float* G, size_t nrow) {
+  constexpr int L = A - 1;
+  constexpr int K = A * A;
+  constexpr int NV = mom_nv<A>(), NVP = mom_nvp<A>();
+  float M0[K], M1[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    M0[k] = 0.f;
+    M1[k] = 0.f;
+  }
+  float W0 = 0.f, W1 = 0.f;
+  for (int a = sl; a < na; a += LPA) {
+    const float4 u = sm.au[a], f = sm.af[a];
+    const float w1 = f.x * f.z;   // fc x spin (zero for a single species)
+    mom_accumulate<L, true>(u.x, u.y, u.z, f.x, w1, M0, M1);
+    W0 = fmaf(f.x, f.x, W0);
+    W1 = fmaf(w1, w1, W1);
+  }
+  __syncwarp(gmask);   // the staged neighbours are consumed: reuse the area
+  float* scr = reinterpret_cast<float*>(sm.au);
+  float4* dst = reinterpret_cast<float4*>(scr + sl * NVP);
+#pragma unroll
+  for (int c4 = 0; c4 < NVP / 4; ++c4) {
+    float v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int c = 4 * c4 + e;
+      v[e] = c < K ? M0[c] : (c < 2 * K ? M1[c - K] : (c == 2 * K ? W0 : (c == 2 * K + 1 ? W1 : 0.f)));
+    }
+    dst[c4] = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  __syncwarp(gmask);
+  float* sq = scr + LPA * NVP;
+  float* Mg = b.M + (size_t)i * b.mom_pad;
+  for (int c = sl; c < NV; c += LPA) {
+    float t = 0.f;
+#pragma unroll
+    for (int r = 0; r < LPA; ++r) t += scr[r * NVP + c];
+    if (c < 2 * K) {
+      if (active) Mg[c] = t;
+      sq[c] = t * t;
+    } else {
+      sq[c] = t;
+    }
+  }
+  __syncwarp(gmask);
+  if (!active || sl >= A) return;
+  float p0[A], p1[A];
+#pragma unroll
+  for (int l = 0; l < A; ++l) {
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int k = l * l; k < (l + 1) * (l + 1); ++k) {
+      s0 += sq[k];
+      s1 += sq[K + k];
+    }
+    p0[l] = s0;
+    p1[l] = s1;
+  }
+  W0 = sq[2 * K];
+  W1 = sq[2 * K + 1];
+  const float* q = pd.qleg + (size_t)ti * AE_MOMA * AE_MOMA;
+#pragma unroll
+  for (int n = 0; n < A; ++n) {
+    if (n % LPA == sl) {
+      float g0 = 0.f, g1 = 0.f, t1 = 0.f;
+#pragma unroll
+      for (int l = 0; l <= n; ++l) {
+        const float ql = q[n * AE_MOMA + l];
+        g0 = fmaf(ql, p0[l], g0);
+        g1 = fmaf(ql, p1[l], g1);
+        t1 += ql;
+      }
+      G[ct.a_i1 + n] = normalise(0.5f * (g0 - t1 * W0), pd, nrow + ct.a_i1 + n);
+      if (multi) G[ct.a_i2 + n] = normalise(0.5f * (g1 - t1 * W1), pd, nrow + ct.a_i2 + n);
+    }
+  }
+}
+
 // ----------------------------------------------------------------------
 // forward
 // ----------------------------------------------------------------------
-template <typename T, int R, int A, int LPA, bool GUARD>
+template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
 __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
@@ -189,7 +297,8 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
   const int gid = wglobal * GPW + grp;
   const bool active = gid < b.natoms;
   const int i = active ? gid : b.natoms - 1;
-  GroupSmem<T> sm = group_smem<T>(smem_raw, b.cap_a, pd.nsf_pad, warp * GPW + grp, false);
+  GroupSmem<T> sm = group_smem<T>(smem_raw, b.cap_a, pd.nsf_pad, warp * GPW + grp, false,
+                                  MOM ? mom_scratch_bytes<A, LPA>() : 0);
   const int ti = b.types[i];
   const ChebTable& ct = pd.sp[ti].cheb;
   const int n = active ? b.nb_cnt[i] : 0;
@@ -291,65 +400,69 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
   }
 
   // ---- angular terms
-  T ang[A], angs[A];
+  if constexpr (MOM) {
+    forward_moments<A, LPA>(pd, b, sm, ct, na, sl, gmask, active, i, ti, multi, G, nrow);
+  } else {
+    T ang[A], angs[A];
 #pragma unroll
-  for (int q = 0; q < A; ++q) {
-    ang[q] = T(0);
-    angs[q] = T(0);
-  }
-  // pairs (a, k = a + t mod na), t = 1 .. na/2, as in the adjoint: the
-  // owner of a keeps it in registers and every pair is visited once
-  const int tmax = na / 2;
-  for (int a0 = 0; a0 < na; a0 += LPA) {
-    const int a = a0 + sl;
-    const bool own = active && a < na;
-    T4 uj, fj;
-    if (own) {
-      uj = sm.au[a];
-      fj = sm.af[a];
-    } else {
-      uj.x = uj.y = uj.z = uj.w = T(0);
-      fj.x = fj.y = fj.z = fj.w = T(0);
+    for (int q = 0; q < A; ++q) {
+      ang[q] = T(0);
+      angs[q] = T(0);
     }
-    for (int t = 1; t <= tmax; ++t) {
-      int k = a + t;
-      if (k >= na) k -= na;
-      if (own && !(2 * t == na && a >= tmax)) {
-        const T4 uk = sm.au[k];
-        const T4 fk = sm.af[k];
-        const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
-        const T w = fj.x * fk.x;
-        const T sw = fj.z * fk.z * w;
-        T x, dxdc;
-        angular_arg(cosv, ct.angular_legacy, x, dxdc);
-        const T x2 = x + x;
-        T tm1 = T(1), t0 = x;
-        ang[0] += w;
-        angs[0] += sw;
+    // pairs (a, k = a + t mod na), t = 1 .. na/2, as in the adjoint: the
+    // owner of a keeps it in registers and every pair is visited once
+    const int tmax = na / 2;
+    for (int a0 = 0; a0 < na; a0 += LPA) {
+      const int a = a0 + sl;
+      const bool own = active && a < na;
+      T4 uj, fj;
+      if (own) {
+        uj = sm.au[a];
+        fj = sm.af[a];
+      } else {
+        uj.x = uj.y = uj.z = uj.w = T(0);
+        fj.x = fj.y = fj.z = fj.w = T(0);
+      }
+      for (int t = 1; t <= tmax; ++t) {
+        int k = a + t;
+        if (k >= na) k -= na;
+        if (own && !(2 * t == na && a >= tmax)) {
+          const T4 uk = sm.au[k];
+          const T4 fk = sm.af[k];
+          const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
+          const T w = fj.x * fk.x;
+          const T sw = fj.z * fk.z * w;
+          T x, dxdc;
+          angular_arg(cosv, ct.angular_legacy, x, dxdc);
+          const T x2 = x + x;
+          T tm1 = T(1), t0 = x;
+          ang[0] += w;
+          angs[0] += sw;
 #pragma unroll
-        for (int q = 1; q < A; ++q) {
-          if (!GUARD || q < aN) {
-            ang[q] = fma(w, t0, ang[q]);
-            angs[q] = fma(sw, t0, angs[q]);
-            const T tn = fma(x2, t0, -tm1);
-            tm1 = t0;
-            t0 = tn;
+          for (int q = 1; q < A; ++q) {
+            if (!GUARD || q < aN) {
+              ang[q] = fma(w, t0, ang[q]);
+              angs[q] = fma(sw, t0, angs[q]);
+              const T tn = fma(x2, t0, -tm1);
+              tm1 = t0;
+              t0 = tn;
+            }
           }
         }
       }
     }
-  }
-#pragma unroll
-  for (int q = 0; q < A; ++q) {
-    ang[q] = gsum<T, LPA>(ang[q]);
-    if (multi) angs[q] = gsum<T, LPA>(angs[q]);
-  }
-  if (active) {
 #pragma unroll
     for (int q = 0; q < A; ++q) {
-      if (q % LPA == sl && q < aN) {
-        G[ct.a_i1 + q] = normalise(ang[q], pd, nrow + ct.a_i1 + q);
-        if (multi) G[ct.a_i2 + q] = normalise(angs[q], pd, nrow + ct.a_i2 + q);
+      ang[q] = gsum<T, LPA>(ang[q]);
+      if (multi) angs[q] = gsum<T, LPA>(angs[q]);
+    }
+    if (active) {
+#pragma unroll
+      for (int q = 0; q < A; ++q) {
+        if (q % LPA == sl && q < aN) {
+          G[ct.a_i1 + q] = normalise(ang[q], pd, nrow + ct.a_i1 + q);
+          if (multi) G[ct.a_i2 + q] = normalise(angs[q], pd, nrow + ct.a_i2 + q);
+        }
       }
     }
   }
@@ -358,7 +471,7 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
 // ----------------------------------------------------------------------
 // adjoint
 // ----------------------------------------------------------------------
-template <typename T, int R, int A, int LPA, bool GUARD>
+template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
 __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
@@ -509,89 +622,161 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
     gav[q] = (!GUARD || q < aN) ? ga[q] : T(0);
     gasv[q] = (multi && (!GUARD || q < aN)) ? gas[q] : T(0);
   }
-  const int tmax = na / 2;
-  for (int a0 = 0; a0 < na; a0 += LPA) {
-    const int a = a0 + sl;
-    const bool own = active && a < na;
-    T4 ua, fa;
-    if (own) {
-      ua = sm.au[a];
-      fa = sm.af[a];
-    } else {
-      ua.x = ua.y = ua.z = T(0);
-      ua.w = T(1);
-      fa.x = fa.y = fa.z = fa.w = T(0);
-    }
-    const T inva = ua.w;
-    T gax = T(0), gay = T(0), gaz = T(0);
-    for (int t = 1; t <= tmax; ++t) {
-      int k = a + t;
-      if (k >= na) k -= na;
-      if (own && !(2 * t == na && a >= tmax)) {
-        const T4 uk = sm.au[k];
-        const T4 fk = sm.af[k];
-        const T cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
-        const T w = fa.x * fk.x;
-        const T ss = fa.z * fk.z;
-        T x, dxdc;
-        angular_arg(cosv, ct.angular_legacy, x, dxdc);
-        const T x2 = x + x;
-        T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
-        T Av = fma(ss, gasv[0], gav[0]), Bv = T(0);
+  if constexpr (MOM) {
+    // moment form: D = B_l M (plain and spin blocks), then one pass over
+    // the staged neighbours, each adding its angular gradient to its
+    // radial force and scattering the total once
+    constexpr int L = A - 1;
+    constexpr int K = A * A;
+    const float* q = pd.qleg + (size_t)ti * AE_MOMA * AE_MOMA;
+    float B0[A], B1[A];
 #pragma unroll
-        for (int q = 1; q < A; ++q) {
-          if (!GUARD || q < aN) {
-            const T cq = fma(ss, gasv[q], gav[q]);
-            Av = fma(cq, t0, Av);
-            Bv = fma(cq * T(q), um1, Bv);
-            const T tn = fma(x2, t0, -tm1);
-            tm1 = t0;
-            t0 = tn;
-            const T un = fma(x2, u0, -um1);
-            um1 = u0;
-            u0 = un;
+    for (int l = 0; l < A; ++l) {
+      B0[l] = 0.f;
+      B1[l] = 0.f;
+    }
+#pragma unroll
+    for (int nn = 0; nn < A; ++nn) {
+#pragma unroll
+      for (int l = 0; l <= nn; ++l) {
+        const float ql = q[nn * AE_MOMA + l];
+        B0[l] = fmaf(gav[nn], ql, B0[l]);
+        B1[l] = fmaf(gasv[nn], ql, B1[l]);
+      }
+    }
+    float tau0 = 0.f, tau1 = 0.f;
+#pragma unroll
+    for (int l = 0; l < A; ++l) {
+      tau0 += B0[l];
+      tau1 += B1[l];
+    }
+    float Mv[4 * ((2 * K + 3) / 4)];
+    const float4* M4 = reinterpret_cast<const float4*>(b.M + (size_t)i * b.mom_pad);
+#pragma unroll
+    for (int c4 = 0; c4 < (2 * K + 3) / 4; ++c4) {
+      const float4 t4 = M4[c4];
+      Mv[4 * c4] = t4.x;
+      Mv[4 * c4 + 1] = t4.y;
+      Mv[4 * c4 + 2] = t4.z;
+      Mv[4 * c4 + 3] = t4.w;
+    }
+    float D0[K], D1[K];
+#pragma unroll
+    for (int l = 0; l < A; ++l) {
+#pragma unroll
+      for (int k = l * l; k < (l + 1) * (l + 1); ++k) {
+        D0[k] = B0[l] * Mv[k];
+        D1[k] = B1[l] * Mv[K + k];
+      }
+    }
+    for (int a = sl; a < na; a += LPA) {
+      if (!active) break;
+      const float4 u = sm.au[a], f = sm.af[a];   // unit vector, 1/d; fc, fc', spin, slot
+      float Fv, px, py, pz;
+      mom_gradient<L, true>(u.x, u.y, u.z, f.z, D0, D1, Fv, px, py, pz);
+      const float up = u.x * px + u.y * py + u.z * pz;
+      const float wd = f.x * u.w;
+      const float cu = f.y * (Fv - (tau0 + tau1 * f.z * f.z) * f.x) - wd * up;
+      const int slot = (int)f.w;
+      const float fx = sm.fbuf[3 * a] - fmaf(cu, u.x, wd * px);
+      const float fy = sm.fbuf[3 * a + 1] - fmaf(cu, u.y, wd * py);
+      const float fz = sm.fbuf[3 * a + 2] - fmaf(cu, u.z, wd * pz);
+      atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
+      fix -= fx;
+      fiy -= fy;
+      fiz -= fz;
+      if (want_virial) {
+        const T4 v = vec[slot];
+        w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
+        w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
+        w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
+      }
+    }
+  } else {
+    const int tmax = na / 2;
+    for (int a0 = 0; a0 < na; a0 += LPA) {
+      const int a = a0 + sl;
+      const bool own = active && a < na;
+      T4 ua, fa;
+      if (own) {
+        ua = sm.au[a];
+        fa = sm.af[a];
+      } else {
+        ua.x = ua.y = ua.z = T(0);
+        ua.w = T(1);
+        fa.x = fa.y = fa.z = fa.w = T(0);
+      }
+      const T inva = ua.w;
+      T gax = T(0), gay = T(0), gaz = T(0);
+      for (int t = 1; t <= tmax; ++t) {
+        int k = a + t;
+        if (k >= na) k -= na;
+        if (own && !(2 * t == na && a >= tmax)) {
+          const T4 uk = sm.au[k];
+          const T4 fk = sm.af[k];
+          const T cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
+          const T w = fa.x * fk.x;
+          const T ss = fa.z * fk.z;
+          T x, dxdc;
+          angular_arg(cosv, ct.angular_legacy, x, dxdc);
+          const T x2 = x + x;
+          T tm1 = T(1), t0 = x, um1 = T(1), u0 = x2;
+          T Av = fma(ss, gasv[0], gav[0]), Bv = T(0);
+#pragma unroll
+          for (int q = 1; q < A; ++q) {
+            if (!GUARD || q < aN) {
+              const T cq = fma(ss, gasv[q], gav[q]);
+              Av = fma(cq, t0, Av);
+              Bv = fma(cq * T(q), um1, Bv);
+              const T tn = fma(x2, t0, -tm1);
+              tm1 = t0;
+              t0 = tn;
+              const T un = fma(x2, u0, -um1);
+              um1 = u0;
+              u0 = un;
+            }
           }
+          const T invk = uk.w;
+          const T Bc = w * Bv * dxdc;
+          const T dEda = fa.y * fk.x * Av, ca = Bc * inva;   // d/dd_a of w A, (dE/dcos)/d_a
+          const T dEdk = fa.x * fk.y * Av, ck = Bc * invk;
+          const T gx = dEda * ua.x + ca * (uk.x - cosv * ua.x);
+          const T gy = dEda * ua.y + ca * (uk.y - cosv * ua.y);
+          const T gz = dEda * ua.z + ca * (uk.z - cosv * ua.z);
+          const T hx = dEdk * uk.x + ck * (ua.x - cosv * uk.x);
+          const T hy = dEdk * uk.y + ck * (ua.y - cosv * uk.y);
+          const T hz = dEdk * uk.z + ck * (ua.z - cosv * uk.z);
+          gax += gx;
+          gay += gy;
+          gaz += gz;
+          sm.fbuf[3 * k] -= hx;
+          sm.fbuf[3 * k + 1] -= hy;
+          sm.fbuf[3 * k + 2] -= hz;
         }
-        const T invk = uk.w;
-        const T Bc = w * Bv * dxdc;
-        const T dEda = fa.y * fk.x * Av, ca = Bc * inva;   // d/dd_a of w A, (dE/dcos)/d_a
-        const T dEdk = fa.x * fk.y * Av, ck = Bc * invk;
-        const T gx = dEda * ua.x + ca * (uk.x - cosv * ua.x);
-        const T gy = dEda * ua.y + ca * (uk.y - cosv * ua.y);
-        const T gz = dEda * ua.z + ca * (uk.z - cosv * ua.z);
-        const T hx = dEdk * uk.x + ck * (ua.x - cosv * uk.x);
-        const T hy = dEdk * uk.y + ck * (ua.y - cosv * uk.y);
-        const T hz = dEdk * uk.z + ck * (ua.z - cosv * uk.z);
-        gax += gx;
-        gay += gy;
-        gaz += gz;
-        sm.fbuf[3 * k] -= hx;
-        sm.fbuf[3 * k + 1] -= hy;
-        sm.fbuf[3 * k + 2] -= hz;
+        __syncwarp(gmask);
+      }
+      if (own) {
+        sm.fbuf[3 * a] -= gax;
+        sm.fbuf[3 * a + 1] -= gay;
+        sm.fbuf[3 * a + 2] -= gaz;
       }
       __syncwarp(gmask);
     }
-    if (own) {
-      sm.fbuf[3 * a] -= gax;
-      sm.fbuf[3 * a + 1] -= gay;
-      sm.fbuf[3 * a + 2] -= gaz;
-    }
-    __syncwarp(gmask);
-  }
-  // forces on the staged neighbours (radial + angular), one scatter each
-  for (int a = sl; a < na; a += LPA) {
-    if (!active) break;
-    const int slot = (int)sm.af[a].w;
-    const T fx = sm.fbuf[3 * a], fy = sm.fbuf[3 * a + 1], fz = sm.fbuf[3 * a + 2];
-    atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
-    fix -= fx;   // the central atom takes minus the neighbour's force
-    fiy -= fy;
-    fiz -= fz;
-    if (want_virial) {
-      const T4 v = vec[slot];
-      w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
-      w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
-      w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
+    // forces on the staged neighbours (radial + angular), one scatter each
+    for (int a = sl; a < na; a += LPA) {
+      if (!active) break;
+      const int slot = (int)sm.af[a].w;
+      const T fx = sm.fbuf[3 * a], fy = sm.fbuf[3 * a + 1], fz = sm.fbuf[3 * a + 2];
+      atomic_add3<T>(F, jt[slot] & AE_INDEX_MASK, fx, fy, fz);
+      fix -= fx;   // the central atom takes minus the neighbour's force
+      fiy -= fy;
+      fiz -= fz;
+      if (want_virial) {
+        const T4 v = vec[slot];
+        w00 += v.x * fx; w01 += v.x * fy; w02 += v.x * fz;
+        w10 += v.y * fx; w11 += v.y * fy; w12 += v.y * fz;
+        w20 += v.z * fx; w21 += v.z * fy; w22 += v.z * fz;
+      }
     }
   }
   fix = gsum<T, LPA>(fix);
@@ -610,21 +795,23 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
   }
 }
 
-template <typename T, int R, int A, int LPA, bool GUARD>
+template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
 int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
   const int warps = 4;
   const int groups = warps * (32 / LPA);
-  size_t smem = group_smem_bytes<T>(b.cap_a, pd.nsf_pad, adjoint) * groups;
+  size_t scratch = 0;
+  if constexpr (MOM) scratch = adjoint ? 0 : mom_scratch_bytes<A, LPA>();
+  size_t smem = group_smem_bytes<T>(b.cap_a, pd.nsf_pad, adjoint, scratch) * groups;
   if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
   const int atoms_per_block = groups;
   const int blocks = (b.natoms + atoms_per_block - 1) / atoms_per_block;
   if (adjoint) {
-    auto kern = k_adjoint<T, R, A, LPA, GUARD>;
+    auto kern = k_adjoint<T, R, A, LPA, GUARD, MOM>;
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<blocks, warps * 32, smem, s>>>(pd, b);
   } else {
-    auto kern = k_forward<T, R, A, LPA, GUARD>;
+    auto kern = k_forward<T, R, A, LPA, GUARD, MOM>;
     if (smem > 48 * 1024)
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<blocks, warps * 32, smem, s>>>(pd, b);
@@ -632,34 +819,53 @@ int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t
   return (int)cudaGetLastError();
 }
 
-template <typename T, int R, int A>
+template <typename T, int R, int A, bool MOM>
 int launch_lpa(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
   switch (b.lpa) {
-    case 8: return launch<T, R, A, 8, false>(pd, b, adjoint, s);
-    case 32: return launch<T, R, A, 32, false>(pd, b, adjoint, s);
-    default: return launch<T, R, A, 16, false>(pd, b, adjoint, s);
+    case 8: return launch<T, R, A, 8, false, MOM>(pd, b, adjoint, s);
+    case 32: return launch<T, R, A, 32, false, MOM>(pd, b, adjoint, s);
+    default: return launch<T, R, A, 16, false, MOM>(pd, b, adjoint, s);
   }
 }
 
-// Exact instantiations for the common (radial, angular) sizes, guarded
-// ones for everything else.
-template <typename T>
-int dispatch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
-  int rN = 0, aN = 0;
+// common (radial, angular) sizes of every species, or false
+inline bool uniform_sizes(const PotDevice& pd, int& rN, int& aN) {
+  rN = aN = 0;
   bool same = true;
   for (int t = 0; t < pd.ntypes; ++t) {
     if (t > 0 && (pd.sp[t].cheb.r_N != rN || pd.sp[t].cheb.a_N != aN)) same = false;
     rN = max(rN, pd.sp[t].cheb.r_N);
     aN = max(aN, pd.sp[t].cheb.a_N);
   }
-  if (same) {
-    if (rN == 11 && aN == 5) return launch_lpa<T, 11, 5>(pd, b, adjoint, s);
-    if (rN == 13 && aN == 7) return launch_lpa<T, 13, 7>(pd, b, adjoint, s);
-    if (rN == 17 && aN == 9) return launch_lpa<T, 17, 9>(pd, b, adjoint, s);
-    if (rN == 17 && aN == 5) return launch_lpa<T, 17, 5>(pd, b, adjoint, s);
+  return same;
+}
+
+// FP32 moment form of the angular terms (k_cheb_mom.cu); returns
+// AE_MOM_NA when the sizes have no moment instantiation
+constexpr int AE_MOM_NA = -1;
+int dispatch_moments(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s);
+
+// Exact instantiations for the common (radial, angular) sizes, guarded
+// ones for everything else.  FP32 evaluations with a moment buffer take
+// the moment form where it is instantiated.
+template <typename T>
+int dispatch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (b.M && pd.qleg) {
+      const int e = dispatch_moments(pd, b, adjoint, s);
+      if (e != AE_MOM_NA) return e;
+    }
   }
-  if (rN <= 24 && aN <= 16) return launch<T, 24, 16, 16, true>(pd, b, adjoint, s);
-  if (rN <= 32 && aN <= 32) return launch<T, 32, 32, 16, true>(pd, b, adjoint, s);
+  int rN, aN;
+  const bool same = uniform_sizes(pd, rN, aN);
+  if (same) {
+    if (rN == 11 && aN == 5) return launch_lpa<T, 11, 5, false>(pd, b, adjoint, s);
+    if (rN == 13 && aN == 7) return launch_lpa<T, 13, 7, false>(pd, b, adjoint, s);
+    if (rN == 17 && aN == 9) return launch_lpa<T, 17, 9, false>(pd, b, adjoint, s);
+    if (rN == 17 && aN == 5) return launch_lpa<T, 17, 5, false>(pd, b, adjoint, s);
+  }
+  if (rN <= 24 && aN <= 16) return launch<T, 24, 16, 16, true, false>(pd, b, adjoint, s);
+  if (rN <= 32 && aN <= 32) return launch<T, 32, 32, 16, true, false>(pd, b, adjoint, s);
   return (int)cudaErrorInvalidValue;
 }
 

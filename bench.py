@@ -63,6 +63,8 @@ def parse():
                     help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
     ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom"],
                     help="fix the neighbour-search kernel (implies --no-tune)")
+    ap.add_argument("--angular-terms", default="moments", choices=["moments", "pairs"],
+                    help="mixed-path angular Chebyshev terms (moment form or pair sums)")
     ap.add_argument("--no-md", action="store_true", help="skip the 1M-atom MD leg")
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
@@ -277,6 +279,7 @@ def run_gb300(args):
     stream = torch.cuda.current_stream()
     tuned = None
     from aenet_gb300 import core as _core
+    _core.set_option("angular_terms", args.angular_terms)
     if args.lanes_per_atom or args.cell_div or args.neighbour_kernel:
         args.no_tune = True
         if args.lanes_per_atom:
@@ -523,6 +526,7 @@ def run_gb300(args):
                                  "per-step working set > 1 GB",
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "cuda_graph": not args.no_graph,
+                           "angular_terms": args.angular_terms,
                            "launch_shape": tuned},
                 "fp64": {"value": value64, "unit": "atoms/s", "ms_per_step": ms64},
                 "mixed_over_fp64": value / value64,

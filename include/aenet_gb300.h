@@ -50,6 +50,11 @@ extern "C" {
  *   "networks" = "tensor" | "simt"   mixed-path networks on the tcgen05
  *       tensor cores (split BF16, FP32 accumulation; networks with two
  *       hidden layers and widths up to 64) or on FP32 SIMT.
+ *   "angular_terms" = "moments" | "pairs"   mixed-path angular Chebyshev
+ *       terms from per-atom moments of real spherical harmonics (the pair
+ *       sum rewritten by the addition theorem; cost linear in the angular
+ *       neighbours, angular orders up to 6) or from the pair sum itself.
+ *       Same values up to FP32 rounding; the FP64 path always sums pairs.
  * Returns AENET_OK or AENET_ERR_INPUT.  Takes effect at the next load or
  * plan creation. */
 int aenet_gpu_set_option(const char* key, const char* value);

@@ -525,3 +525,49 @@ def test_k5_rotation_invariance_and_fcc_shell_on_gpu(cuda, cu256):
         plan.close()
     finally:
         ann.release()
+
+
+@pytest.mark.parametrize("case", ["lisio", "lisio_legacy", "lisio_a7", "cu256"])
+def test_angular_moment_form_matches_pairs(cuda, oracle, cu256, tmp_path, case):
+    """FP32 angular terms in moment form (power spectra of the neighbours'
+    harmonics, linear in the neighbour count) against the FP32 pair sums
+    and the FP64 path: energies, forces and virials for angular orders 4
+    and 6, the current and the legacy angular domain, one and three
+    species."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    angular = "legacy" if case == "lisio_legacy" else "current"
+    if case == "cu256":
+        w, paths = cu256
+    else:
+        w = workloads.lisio_batch_4096(nstruc=24)
+        if case == "lisio_a7":
+            w.setups = workloads.cheb_setups(w.types, 12, 6.0, 6, 4.0)
+            w.networks = workloads.glorot_networks(np.random.default_rng(7), w.types,
+                                                   [40, 32, 32, 1])
+        paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    ann = _ann(paths, w.types, angular)
+    try:
+        structs = [(s.positions, s.types, s.cell, True) for s in w.structures]
+        r64 = ann.batch_energy_forces(structs, precision=FP64, virial=True)
+        out = {}
+        for mode in ("pairs", "moments"):
+            set_option("angular_terms", mode)
+            out[mode] = ann.batch_energy_forces(structs, precision=MIXED, virial=True)
+    finally:
+        set_option("angular_terms", "moments")
+        ann.release()
+    nat = np.array([s.natoms for s in w.structures])
+    for mode in ("pairs", "moments"):
+        dE = np.abs(out[mode]["energy"] - r64["energy"]) / nat
+        dF = out[mode]["forces"] - r64["forces"]
+        assert dE.max() < E_TOL_MIXED, (mode, dE.max())
+        assert np.sqrt((dF ** 2).mean()) < F_RMS_MIXED, mode
+    # both FP32 forms round differently but evaluate the same sums
+    scale_F = np.sqrt((r64["forces"] ** 2).mean())
+    dE = np.abs(out["moments"]["energy"] - out["pairs"]["energy"]) / nat
+    assert dE.max() < 2e-5, dE.max()
+    dF = out["moments"]["forces"] - out["pairs"]["forces"]
+    assert np.sqrt((dF ** 2).mean()) < 1e-4 * max(1.0, scale_F)
+    dV = out["moments"]["virial"] - r64["virial"]
+    assert np.abs(dV).max() < 1e-3 * max(1.0, np.abs(r64["virial"]).max())
