@@ -180,6 +180,23 @@ struct PairWalk {
   }
 };
 
+// Bulk prefetch of an atom's neighbour rows into L2 (one instruction per
+// row, issued by the group's first lane): the radial rounds then wait on L2
+// instead of DRAM.  Rows start 16-byte aligned (the ELL capacity is a
+// multiple of 32) and the sizes are rounded up to 16 bytes inside the row.
+template <typename T4>
+__device__ __forceinline__ void prefetch_rows(const T4* vec, const int* jt, int n) {
+  if (n <= 0) return;
+  const unsigned bv = (unsigned)(sizeof(T4) * n);
+  const unsigned bj = (unsigned)((4 * n + 15) & ~15);
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(vec)),
+               "r"(bv)
+               : "memory");
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(jt)),
+               "r"(bj)
+               : "memory");
+}
+
 template <typename T>
 __device__ __forceinline__ void atomic_add3(T* F, int atom, T fx, T fy, T fz);
 template <>
@@ -284,8 +301,17 @@ __device__ __forceinline__ void forward_moments(const PotDevice& pd, const DescB
 // ----------------------------------------------------------------------
 // forward
 // ----------------------------------------------------------------------
+// resident blocks per SM asked of the register allocator (moment form)
+#ifndef AE_MOM_FWD_BLOCKS
+#define AE_MOM_FWD_BLOCKS 6
+#endif
+#ifndef AE_MOM_ADJ_BLOCKS
+#define AE_MOM_ADJ_BLOCKS 5
+#endif
+
 template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
-__global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
+__global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(PotDevice pd,
+                                                                             DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
   extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -302,9 +328,10 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
   const int ti = b.types[i];
   const ChebTable& ct = pd.sp[ti].cheb;
   const int n = active ? b.nb_cnt[i] : 0;
-  const int nloop = warp_max(n);
   const T4* __restrict__ vec = reinterpret_cast<const T4*>(b.nb_vec) + (size_t)i * b.cap;
   const int* __restrict__ jt = b.nb_jt + (size_t)i * b.cap;
+  if (sl == 0) prefetch_rows(vec, jt, n);
+  const int nloop = warp_max(n);
   const T r_Rc = T(ct.r_Rc), a_Rc = T(ct.a_Rc);
   const T two_over_rc = T(2) / r_Rc;
   const int rN = GUARD ? ct.r_N : R;
@@ -472,7 +499,8 @@ __global__ void __launch_bounds__(128) k_forward(PotDevice pd, DescBuffers b) {
 // adjoint
 // ----------------------------------------------------------------------
 template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
-__global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
+__global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(PotDevice pd,
+                                                                             DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
   extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -488,9 +516,10 @@ __global__ void __launch_bounds__(128) k_adjoint(PotDevice pd, DescBuffers b) {
   const int ti = b.types[i];
   const ChebTable& ct = pd.sp[ti].cheb;
   const int n = active ? b.nb_cnt[i] : 0;
-  const int nloop = warp_max(n);
   const T4* __restrict__ vec = reinterpret_cast<const T4*>(b.nb_vec) + (size_t)i * b.cap;
   const int* __restrict__ jt = b.nb_jt + (size_t)i * b.cap;
+  if (sl == 0) prefetch_rows(vec, jt, n);
+  const int nloop = warp_max(n);
   const T r_Rc = T(ct.r_Rc), a_Rc = T(ct.a_Rc);
   const T two_over_rc = T(2) / r_Rc;
   const int rN = GUARD ? ct.r_N : R;
