@@ -1,7 +1,8 @@
 """Measured choice of the evaluator's launch shapes.
 
 Three knobs decide most of the run time of a batch: the neighbour-search
-kernel (one warp per home cell or per atom), the number of neighbour-search
+kernel (one warp per atom, or per home cell with a lane per home atom or a
+lane per candidate), the number of neighbour-search
 cells per cut-off length (1, 2 or 3) and the number of lanes that cooperate
 on one atom in the descriptor and adjoint kernels (8, 16 or 32).  The first
 two only change the neighbour search and the last only the descriptor
@@ -20,7 +21,7 @@ from .plan import Plan
 
 LANES = (8, 16, 32)
 CELL_DIVS = (1, 2, 3)
-NB_KERNELS = ("cell", "atom")
+NB_KERNELS = ("cell", "atom", "stream")
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "aenet_gb300", "autotune.json")
 
 

@@ -204,7 +204,8 @@ struct NbBuffers {
   void* nb_vec;               // float4 or double4_32a
   int* nb_img;                // optional: image T packed 3 x 10-bit signed
   unsigned* status;
-  int cell_kernel;            // 1: one warp per home cell, 0: one warp per atom
+  int cell_kernel;            // 0: warp per atom; warp per home cell with a lane per
+                              // home atom (1) or a lane per candidate (2)
 };
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types,

@@ -186,6 +186,12 @@ __device__ __forceinline__ int floor_div_r(int a, float inv_n) {
   return (int)floorf(((float)a + 0.5f) * inv_n);
 }
 
+// |R| of an accepted FP32 pair from the squared length (one reciprocal
+// square root; zero length stays zero)
+__device__ __forceinline__ float pair_length(float dd2) {
+  return dd2 > 0.f ? dd2 * rsqrtf(dd2) : 0.f;
+}
+
 __device__ __forceinline__ int floor_div(int a, int n) {
   int q = a / n;
   return (a % n != 0 && (a < 0)) ? q - 1 : q;
@@ -219,8 +225,8 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
   const int packed = nb.cell_of[i];
   const int c0 = packed & 1023, c1 = (packed >> 10) & 1023, c2 = (packed >> 20) & 1023;
   // images along the third axis reachable from this cell
-  const int t2lo = pbc ? floor_div(c2 - k2, nc2) : 0;
-  const int t2hi = pbc ? floor_div(c2 + k2, nc2) : 0;
+  const int t2lo = pbc ? floor_div_r(c2 - k2, g->inv_nc[2]) : 0;
+  const int t2hi = pbc ? floor_div_r(c2 + k2, g->inv_nc[2]) : 0;
   const int nt2 = t2hi - t2lo + 1;
   const int nunits = (2 * k0 + 1) * w1 * nt2;
   const float4 ri = nb.r_f32[i];
@@ -323,9 +329,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
       const int own = upto ? su_first[warp][31 - __clz(upto)] : carry;
       carry = __shfl_sync(0xffffffffu, own, 31);
       const float4 osh = su_sh[warp][own];
-      const int img = __float_as_int(osh.w);
-      const int oT0 = sext10i(img & 1023), oT1 = sext10i((img >> 10) & 1023),
-                oT2 = sext10i((img >> 20) & 1023);
+      const int img = __float_as_int(osh.w);   // packed image; zero for T = 0
       const float osh0 = osh.x, osh1 = osh.y, osh2 = osh.z;
       bool accept = false;
       int j = -1, tj = 0;
@@ -336,7 +340,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
         j = nb.cell_atoms[p];
         tj = __float_as_int(rj.w);
         const bool self_img = (j == i);
-        const bool zeroT = (oT0 == 0 && oT1 == 0 && oT2 == 0);
+        const bool zeroT = img == 0;
         if (!(self_img && zeroT)) {
           dx = (rj.x - ri.x) + osh0;
           dy = (rj.y - ri.y) + osh1;
@@ -346,6 +350,8 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
             accept = true;
           } else if (dd2 <= rc2_hi) {
             // exact FP64 predicate, evaluated as the reference does
+            const int oT0 = sext10i(img & 1023), oT1 = sext10i((img >> 10) & 1023),
+                      oT2 = sext10i((img >> 20) & 1023);
             double e2;
             if (pbc) {
               double cart[3];
@@ -383,11 +389,12 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
         const int k = cnt + __popc(mask & ((1u << lane) - 1u));
         if (k < cap) {
           nb.nb_jt[row + k] = j | (tj << AE_TYPE_SHIFT);
-          if (nb.nb_img)
-            nb.nb_img[row + k] = (oT0 & 1023) | ((oT1 & 1023) << 10) | ((oT2 & 1023) << 20);
+          if (nb.nb_img) nb.nb_img[row + k] = img;
           if (VecOut<T4>::fp64) {
             // R_ij = L (s_j + T) - L s_i in FP64 (the vectors the reference's
             // descriptor sees)
+            const int oT0 = sext10i(img & 1023), oT1 = sext10i((img >> 10) & 1023),
+                      oT2 = sext10i((img >> 20) & 1023);
             double R[3];
             if (pbc) {
               const double* sj = nb.s_wrap + 3 * j;
@@ -406,7 +413,8 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
             reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] =
                 make_double4_32a(R[0], R[1], R[2], dist);
           } else {
-            reinterpret_cast<float4*>(nb.nb_vec)[row + k] = make_float4(dx, dy, dz, sqrtf(dd2));
+            reinterpret_cast<float4*>(nb.nb_vec)[row + k] =
+                make_float4(dx, dy, dz, pair_length(dd2));
           }
         }
       }
@@ -453,8 +461,8 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
   const int w1 = 2 * k1 + 1;
   const int lin = gc - g->cell_off;
   const int c2 = lin % nc2, c1 = (lin / nc2) % nc1, c0 = lin / (nc1 * nc2);
-  const int t2lo = pbc ? floor_div(c2 - k2, nc2) : 0;
-  const int t2hi = pbc ? floor_div(c2 + k2, nc2) : 0;
+  const int t2lo = pbc ? floor_div_r(c2 - k2, g->inv_nc[2]) : 0;
+  const int t2hi = pbc ? floor_div_r(c2 + k2, g->inv_nc[2]) : 0;
   const int nt2 = t2hi - t2lo + 1;
   const int nunits = (2 * k0 + 1) * w1 * nt2;
   const float rc2_lo = g->rc2_lo, rc2_hi = g->rc2_hi;
@@ -641,6 +649,250 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
   }
 }
 
+// ---- candidate-streaming search: one warp per home cell, lane = candidate.
+// The stencil units of the home cell (pruned for the whole cell in
+// orthogonal cells, as above) are flattened into batches of 32 candidates
+// held one per lane; every batch is tested against each home atom of the
+// cell in turn (home positions broadcast from shared memory), accepted
+// pairs compacted by ballot into the home atom's row.  The unit mapping and
+// the candidate loads are shared by all atoms of the cell, and all lanes
+// stay busy however few atoms a cell holds.  Same FP32 filter + FP64 band
+// test as the other kernels.
+constexpr int NBS_WARPS = 8;
+
+// the reference's FP64 predicate for a pair in the band around the cut-off
+__device__ __forceinline__ bool band_accept(const StructGeom* g, const NbBuffers& nb, int pbc,
+                                            int ih, int j, int t0, int t1, int t2, double rc2) {
+  double e2;
+  if (pbc) {
+    double cart[3];
+    if (j == ih) {
+      for (int cc = 0; cc < 3; ++cc) {
+        double t = dm(g->L[cc], (double)t0);
+        t = da(t, dm(g->L[3 + cc], (double)t1));
+        t = da(t, dm(g->L[6 + cc], (double)t2));
+        cart[cc] = t;
+      }
+    } else {
+      const double* sj = nb.s_wrap + 3 * j;
+      const double u0 = da(sj[0], (double)t0), u1 = da(sj[1], (double)t1),
+                   u2 = da(sj[2], (double)t2);
+      for (int cc = 0; cc < 3; ++cc) {
+        double t = dm(g->L[cc], u0);
+        t = da(t, dm(g->L[3 + cc], u1));
+        t = da(t, dm(g->L[6 + cc], u2));
+        cart[cc] = da(t, -nb.r_wrap[3 * ih + cc]);
+      }
+    }
+    e2 = da(da(dm(cart[0], cart[0]), dm(cart[1], cart[1])), dm(cart[2], cart[2]));
+  } else {
+    const double c0d = da(nb.r_wrap[3 * j], -nb.r_wrap[3 * ih]);
+    const double c1d = da(nb.r_wrap[3 * j + 1], -nb.r_wrap[3 * ih + 1]);
+    const double c2d = da(nb.r_wrap[3 * j + 2], -nb.r_wrap[3 * ih + 2]);
+    e2 = da(da(dm(c0d, c0d), dm(c1d, c1d)), dm(c2d, c2d));
+  }
+  return e2 <= rc2;
+}
+
+// R_ij = L (s_j + T) - L s_i in FP64 and its length
+__device__ __forceinline__ double4_32a fp64_pair_vector(const StructGeom* g, const NbBuffers& nb,
+                                                        int pbc, int ih, int j, int t0, int t1,
+                                                        int t2) {
+  double R[3];
+  if (pbc) {
+    const double* sj = nb.s_wrap + 3 * j;
+    const double u0 = da(sj[0], (double)t0), u1 = da(sj[1], (double)t1),
+                 u2 = da(sj[2], (double)t2);
+    for (int cc = 0; cc < 3; ++cc) {
+      double t = dm(g->L[cc], u0);
+      t = da(t, dm(g->L[3 + cc], u1));
+      t = da(t, dm(g->L[6 + cc], u2));
+      R[cc] = da(t, -nb.r_wrap[3 * ih + cc]);
+    }
+  } else {
+    for (int cc = 0; cc < 3; ++cc) R[cc] = da(nb.r_wrap[3 * j + cc], -nb.r_wrap[3 * ih + cc]);
+  }
+  const double dist = sqrt(da(da(dm(R[0], R[0]), dm(R[1], R[1])), dm(R[2], R[2])));
+  return make_double4_32a(R[0], R[1], R[2], dist);
+}
+
+template <typename T4>
+__global__ void __launch_bounds__(32 * NBS_WARPS) k_neighbors_stream(int ncells, NbBuffers nb) {
+  __shared__ int su_base[NBS_WARPS][32];
+  __shared__ float4 su_sh[NBS_WARPS][32];
+  __shared__ int su_first[NBS_WARPS][32];
+  __shared__ float4 sh_pos[NBS_WARPS][32];   // home atoms: position, species bits in w
+  __shared__ int sh_i[NBS_WARPS][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gc = blockIdx.x * NBS_WARPS + warp;
+  if (gc >= ncells) return;
+  const int hb = nb.cell_start[gc], he = nb.cell_start[gc + 1];
+  if (hb >= he) return;
+  // the structure of the cell is that of any of its atoms
+  const StructGeom* g = nb.geom + nb.atom_struct[nb.cell_atoms[hb]];
+  const int pbc = g->pbc;
+  const int nc0 = g->nc[0], nc1 = g->nc[1], nc2 = g->nc[2];
+  const int k0 = g->kr[0], k1 = g->kr[1], k2 = g->kr[2];
+  const int w1 = 2 * k1 + 1;
+  const int lin = gc - g->cell_off;
+  const int c2 = lin % nc2, c1 = (lin / nc2) % nc1, c0 = lin / (nc1 * nc2);
+  const int t2lo = pbc ? floor_div_r(c2 - k2, g->inv_nc[2]) : 0;
+  const int t2hi = pbc ? floor_div_r(c2 + k2, g->inv_nc[2]) : 0;
+  const int nt2 = t2hi - t2lo + 1;
+  const int nunits = (2 * k0 + 1) * w1 * nt2;
+  const float rc2_lo = g->rc2_lo, rc2_hi = g->rc2_hi;
+  const double rc2 = g->rc2;
+  const int cap = nb.cap;
+  const int* __restrict__ cstart = nb.cell_start + g->cell_off;
+  const float rcf = g->rcf * 1.0001f + 1e-4f;
+  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const int ortho = g->ortho;
+  const float cw0 = g->hf[0] * g->inv_nc[0], cw1 = g->hf[1] * g->inv_nc[1];
+  const float zsc = g->inv_hf[2] * nc2 * 1.0001f;
+  const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
+  const float* __restrict__ Lf = g->Lf;
+
+  for (int hbase = hb; hbase < he; hbase += 32) {
+    const int nh = min(32, he - hbase);
+    __syncwarp();
+    if (lane < nh) {
+      sh_pos[warp][lane] = nb.cell_pos[hbase + lane];
+      sh_i[warp][lane] = nb.cell_atoms[hbase + lane];
+    }
+    __syncwarp();
+    int cnt = 0;   // lane h: neighbours of home atom h found so far
+    for (int ubase = 0; ubase < nunits; ubase += 32) {
+      const int u = ubase + lane;
+      int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
+      float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
+      if (u < nunits) {
+        const int rr = floor_div_r(u, inv_nt2);
+        const int it2 = u - rr * nt2;
+        const int q0 = floor_div_r(rr, inv_w1);
+        const int d1 = rr - q0 * w1 - k1;
+        const int d0 = q0 - k0;
+        int a0 = c0 + d0, a1 = c1 + d1;
+        bool ok = true;
+        int zlo = c2 - k2, zhi = c2 + k2;
+        if (ortho) {
+          // gap between the home cell and row (a0, a1), whole cells apart
+          const float gx = (float)max(0, abs(d0) - 1) * cw0;
+          const float gy = (float)max(0, abs(d1) - 1) * cw1;
+          const float rem = rcf * rcf - gx * gx - gy * gy;
+          if (rem < 0.f) {
+            ok = false;
+          } else {
+            const int hz = 1 + (int)floorf(sqrtf(rem) * zsc + 1e-4f);
+            zlo = max(zlo, c2 - hz);
+            zhi = min(zhi, c2 + hz);
+          }
+        }
+        if (pbc) {
+          T0 = floor_div_r(a0, inc0);
+          a0 -= T0 * nc0;
+          T1 = floor_div_r(a1, inc1);
+          a1 -= T1 * nc1;
+          T2 = t2lo + it2;
+          zlo = max(zlo, T2 * nc2);
+          zhi = min(zhi, T2 * nc2 + nc2 - 1);
+        } else {
+          ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
+          zlo = max(zlo, 0);
+          zhi = min(zhi, nc2 - 1);
+        }
+        if (ok && zlo <= zhi) {
+          const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
+          beg = cstart[base + zlo];
+          len = cstart[base + zhi + 1] - beg;
+          const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
+          sh0 = f0 * Lf[0] + f1 * Lf[3] + f2 * Lf[6];
+          sh1 = f0 * Lf[1] + f1 * Lf[4] + f2 * Lf[7];
+          sh2 = f0 * Lf[2] + f1 * Lf[5] + f2 * Lf[8];
+        }
+      }
+      int incl = len;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int w = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += w;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      const int start = incl - len;
+      __syncwarp();
+      su_base[warp][lane] = beg - start;
+      su_sh[warp][lane] = make_float4(sh0, sh1, sh2,
+                                      __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) |
+                                                     ((T2 & 1023) << 20)));
+      __syncwarp();
+      int carry = 0;
+      for (int qb = 0; qb < total; qb += 32) {
+        // ---- this lane's candidate (unit lookup as in k_neighbors)
+        const int q = qb + lane;
+        const bool starts = len > 0 && start >= qb && start < qb + 32;
+        __syncwarp();
+        if (starts) su_first[warp][start - qb] = lane;
+        const unsigned marks = __reduce_or_sync(0xffffffffu, starts ? (1u << (start - qb)) : 0u);
+        __syncwarp();
+        const unsigned upto = marks & (0xffffffffu >> (31 - lane));
+        const int own = upto ? su_first[warp][31 - __clz(upto)] : carry;
+        carry = __shfl_sync(0xffffffffu, own, 31);
+        const bool valid = q < total;
+        float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
+        int cj = -1;
+        const float4 cs = su_sh[warp][own];
+        if (valid) {
+          const int p = su_base[warp][own] + q;
+          cp = nb.cell_pos[p];
+          cj = nb.cell_atoms[p];
+        }
+        const int img = __float_as_int(cs.w);
+        const int jt = cj | (__float_as_int(cp.w) << AE_TYPE_SHIFT);
+        // ---- against every home atom of the cell
+        for (int h = 0; h < nh; ++h) {
+          const float4 rh = sh_pos[warp][h];
+          const int ih = sh_i[warp][h];
+          bool acc = false, band = false;
+          float dx = 0.f, dy = 0.f, dz = 0.f, dd2 = 0.f;
+          if (valid && !(cj == ih && img == 0)) {
+            dx = (cp.x - rh.x) + cs.x;
+            dy = (cp.y - rh.y) + cs.y;
+            dz = (cp.z - rh.z) + cs.z;
+            dd2 = dx * dx + dy * dy + dz * dz;
+            acc = dd2 < rc2_lo;
+            band = !acc && dd2 <= rc2_hi;
+          }
+          if (__any_sync(0xffffffffu, band)) {
+            if (band)
+              acc = band_accept(g, nb, pbc, ih, cj, sext10i(img & 1023), sext10i((img >> 10) & 1023),
+                                sext10i((img >> 20) & 1023), rc2);
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, acc);
+          if (m == 0u) continue;
+          const int k = __shfl_sync(0xffffffffu, cnt, h) + __popc(m & ((1u << lane) - 1u));
+          if (acc && k < cap) {
+            const size_t row = (size_t)ih * cap;
+            nb.nb_jt[row + k] = jt;
+            if (nb.nb_img) nb.nb_img[row + k] = img;
+            if (VecOut<T4>::fp64) {
+              reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] = fp64_pair_vector(
+                  g, nb, pbc, ih, cj, sext10i(img & 1023), sext10i((img >> 10) & 1023),
+                  sext10i((img >> 20) & 1023));
+            } else {
+              reinterpret_cast<float4*>(nb.nb_vec)[row + k] =
+                  make_float4(dx, dy, dz, pair_length(dd2));
+            }
+          }
+          if (lane == h) cnt += __popc(m);
+        }
+      }
+    }
+    if (lane < nh) {
+      nb.nb_cnt[sh_i[warp][lane]] = min(cnt, cap);
+      if (cnt > cap) atomicOr(nb.status, AE_ST_NB_OVERFLOW);
+    }
+  }
+}
+
 // ---- caller's neighbour list (CSR over local atoms, indices into local +
 // ghost atoms) -> ELL table.  R_ij = x_j - x_i in FP64; pairs beyond
 // (Rc + 1e-3) are dropped; species from the caller's type ids.
@@ -729,8 +981,15 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
   k_scan_sums<<<1, SCAN_B, 0, s>>>(nblk, nb.scan_tmp, nb.cell_start + nc);
   k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
   k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
+  if (nb.cell_kernel == 2) {
+    const int blocks = (nc + NBS_WARPS - 1) / NBS_WARPS;
+    if (fp64)
+      k_neighbors_stream<double4_32a><<<blocks, 32 * NBS_WARPS, 0, s>>>(nc, nb);
+    else
+      k_neighbors_stream<float4><<<blocks, 32 * NBS_WARPS, 0, s>>>(nc, nb);
+    return (int)cudaGetLastError();
+  }
   if (nb.cell_kernel) {
-    // zero counts first: empty home cells launch no work for their atoms
     const int blocks = (nc + NBC_WARPS - 1) / NBC_WARPS;
     if (fp64)
       k_neighbors_cell<double4_32a><<<blocks, 32 * NBC_WARPS, 0, s>>>(nc, nb);

@@ -61,7 +61,7 @@ def parse():
                     help="fix the descriptor kernels' lanes per atom (implies --no-tune)")
     ap.add_argument("--cell-div", type=int, default=0,
                     help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
-    ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom"],
+    ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom", "stream"],
                     help="fix the neighbour-search kernel (implies --no-tune)")
     ap.add_argument("--angular-terms", default="moments", choices=["moments", "pairs"],
                     help="mixed-path angular Chebyshev terms (moment form or pair sums)")

@@ -49,10 +49,11 @@ def aucu(oracle, tmp_path_factory):
     return w, paths
 
 
-@pytest.fixture(params=["atom", "cell"])
+@pytest.fixture(params=["atom", "cell", "stream"])
 def nb_kernel(request, cuda):
-    """Run a test with either neighbour-search kernel (one warp per atom or
-    one warp per home cell); restores the default afterwards."""
+    """Run a test with each neighbour-search kernel (one warp per atom, or
+    one warp per home cell with a lane per home atom or per candidate);
+    restores the default afterwards."""
     from aenet_gb300.core import set_option
     set_option("neighbour_kernel", request.param)
     yield request.param
