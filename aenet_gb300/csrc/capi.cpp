@@ -266,6 +266,7 @@ struct State {
   std::vector<HostPot> pots;
   int angular_legacy = 0;
   int cell_div = 2;
+  int z_refine = 1;          // search cells along the third axis per cell_div cell
   int lpa_default = 16;
   int lpa_adjoint = 0;        // lanes per atom of the adjoint (0: as the forward)
   int networks_tc = 1;       // tensor-core networks on the mixed path when eligible
@@ -815,6 +816,7 @@ struct aenet_gpu_plan {
   std::vector<int> pbc_h;
   const PotDevice* pd = nullptr;   // tables used by this plan
   int cell_div = 2;
+  int z_refine = 1;
   double rc = 0;
   // device memory
   void* mem = nullptr;
@@ -903,8 +905,12 @@ void cross(const double* a, const double* b, double* c) {
 }
 
 // geometry of one structure
+// Cells of the search grid are rcp/cell_div wide along the first two axes
+// and z_refine times narrower along the third: stencil rows keep their
+// number while the cut of each row to the cut-off sphere gets finer.
 int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, int natoms,
-              double rc, int cell_div, int frac_mode, const int* force_nc = nullptr) {
+              double rc, int cell_div, int frac_mode, const int* force_nc = nullptr,
+              int z_refine = 1) {
   memset(&G, 0, sizeof(G));
   G.pbc = pbc;
   G.frac_mode = frac_mode;
@@ -945,7 +951,7 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
       double bl = std::sqrt(bb[a][0] * bb[a][0] + bb[a][1] * bb[a][1] + bb[a][2] * bb[a][2]);
       double h = std::fabs(V) / bl;   // height of the cell along axis a
       G.hf[a] = (float)h;
-      int nc = (int)std::floor(h / w);
+      int nc = (int)std::floor(h / (a == 2 ? w / z_refine : w));
       if (nc < 1) nc = 1;
       if (nc > 1000) nc = 1000;
       if (force_nc) nc = force_nc[a];
@@ -972,7 +978,7 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
       G.box[c] = (mx[c] - mn[c]) + rcp;
       G.hf[c] = (float)G.box[c];
       G.L[4 * c] = G.box[c];
-      int nc = (int)std::floor(G.box[c] / w);
+      int nc = (int)std::floor(G.box[c] / (c == 2 ? w / z_refine : w));
       if (nc < 1) nc = 1;
       if (nc > 1000) nc = 1000;
       G.nc[c] = nc;
@@ -1004,7 +1010,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
     StructGeom& G = P->geom_h[s];
     const double* c0 = coords0 ? coords0 + 3 * (size_t)atom_off : nullptr;
     int st = make_geom(G, lattices ? lattices + 9 * (size_t)s : nullptr, P->pbc_h[s], c0,
-                       P->natoms_h[s], rc, P->cell_div, 0);
+                       P->natoms_h[s], rc, P->cell_div, 0, nullptr, P->z_refine);
     if (st) return st;
     int nc = G.nc[0] * G.nc[1] * G.nc[2];
     G.cell_off = cell_off;
@@ -1154,6 +1160,7 @@ aenet_gpu_plan* plan_new(int nstruc, const int* natoms, const double* lattices, 
   P->pd = pd;
   P->rc = rc;
   P->cell_div = g.cell_div;
+  P->z_refine = g.z_refine;
   P->cap = cap;
   P->cap_a = cap > 0 ? cap : 0;   // an explicit capacity (a retry) stages every neighbour
   P->keep_images = keep_images;
@@ -1771,10 +1778,11 @@ EXPORT void aenet_nbl_init(double latt_vec[9], int natoms, int atom_types[], dou
     Pn->pd = nullptr;
     Pn->rc = aenet_Rc_max;
     Pn->cell_div = g.cell_div;
+    Pn->z_refine = g.z_refine;
     Pn->keep_images = true;
     // isolated structures are binned on the Cartesian input
     int st = make_geom(Pn->geom_h[0], latt_vec, pbcv, coords, nat, aenet_Rc_max, g.cell_div,
-                       cartesian ? 1 : 2);
+                       cartesian ? 1 : 2, nullptr, g.z_refine);
     if (st) return;
     // plan_alloc recomputes the geometry with frac_mode 0; redo with the
     // nbl convention afterwards
@@ -1900,6 +1908,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     g.lpa_default = d;
     return AENET_OK;
   }
+  if (k == "z_refine") {
+    int d = atoi(v.c_str());
+    if (d < 1 || d > 4) return AENET_ERR_INPUT;
+    g.z_refine = d;
+    return AENET_OK;
+  }
   if (k == "cell_div") {
     int d = atoi(v.c_str());
     if (d < 1 || d > 3) return AENET_ERR_INPUT;
@@ -1962,7 +1976,7 @@ EXPORT int aenet_gpu_plan_set_lattices(aenet_gpu_plan* P, const double* lattices
     // the cell grid keeps its dimensions (the slot layout depends on them);
     // the stencil half widths follow the new heights
     int st = make_geom(G, lattices + 9 * (size_t)s, 1, nullptr, P->natoms_h[s], P->rc, P->cell_div,
-                       O.frac_mode, O.nc);
+                       O.frac_mode, O.nc, P->z_refine);
     if (st) return st;
     G.cell_off = O.cell_off;
     G.atom_off = O.atom_off;

@@ -63,6 +63,8 @@ def parse():
                     help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
     ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom", "stream"],
                     help="fix the neighbour-search kernel (implies --no-tune)")
+    ap.add_argument("--z-refine", type=int, default=0,
+                    help="search cells this many times narrower along the third axis")
     ap.add_argument("--angular-terms", default="moments", choices=["moments", "pairs"],
                     help="mixed-path angular Chebyshev terms (moment form or pair sums)")
     ap.add_argument("--no-md", action="store_true", help="skip the 1M-atom MD leg")
@@ -280,8 +282,10 @@ def run_gb300(args):
     tuned = None
     from aenet_gb300 import core as _core
     _core.set_option("angular_terms", args.angular_terms)
-    if args.lanes_per_atom or args.cell_div or args.neighbour_kernel:
+    if args.lanes_per_atom or args.cell_div or args.neighbour_kernel or args.z_refine:
         args.no_tune = True
+        if args.z_refine:
+            _core.set_option("z_refine", args.z_refine)
         if args.lanes_per_atom:
             _core.set_option("lanes_per_atom", args.lanes_per_atom)
         if args.cell_div:
@@ -289,6 +293,7 @@ def run_gb300(args):
         if args.neighbour_kernel:
             _core.set_option("neighbour_kernel", args.neighbour_kernel)
         tuned = {"lanes_per_atom": args.lanes_per_atom or None, "cell_div": args.cell_div or None,
+                 "z_refine": args.z_refine or None,
                  "neighbour_kernel": args.neighbour_kernel or None, "fixed": True}
     if not args.no_tune:
         from aenet_gb300 import autotune

@@ -41,6 +41,9 @@ extern "C" {
  *                potentials shipped with aenet were trained with.
  *   "cell_div" = "1" | "2" | "3"   cells per cut-off length in the
  *       neighbour search grid (performance only).
+ *   "z_refine" = "1" .. "4"   the search cells are that many times narrower
+ *       along the third lattice axis: the same stencil rows, each cut more
+ *       finely to the cut-off sphere (performance only).
  *   "lanes_per_atom" = "8" | "16" | "32"   descriptor kernels' lanes per
  *       atom (performance only).
  *   "neighbour_kernel" = "atom" | "cell" | "stream"   neighbour search

@@ -49,15 +49,19 @@ def aucu(oracle, tmp_path_factory):
     return w, paths
 
 
-@pytest.fixture(params=["atom", "cell", "stream"])
+@pytest.fixture(params=["atom", "cell", "stream", "atom_z4", "stream_z2"])
 def nb_kernel(request, cuda):
     """Run a test with each neighbour-search kernel (one warp per atom, or
-    one warp per home cell with a lane per home atom or per candidate);
-    restores the default afterwards."""
+    one warp per home cell with a lane per home atom or per candidate),
+    also on grids refined along the third axis; restores the defaults
+    afterwards."""
     from aenet_gb300.core import set_option
-    set_option("neighbour_kernel", request.param)
+    kernel, _, z = request.param.partition("_z")
+    set_option("neighbour_kernel", kernel)
+    set_option("z_refine", int(z or 1))
     yield request.param
     set_option("neighbour_kernel", "atom")
+    set_option("z_refine", 1)
 
 
 def _ann(paths, types, angular=None):
