@@ -164,7 +164,9 @@ def neighbour_stats(plan, a_rc, r_rc):
 
 
 def cheb_flops(nb, R, A, nsf, m, arch):
-    """Canonical per-atom flop counts of the survey's measurement section."""
+    """Per-atom flop counts of the reference's pair-form algorithm (radial
+    terms per neighbour, angular terms per pair): the moment form does
+    fewer, so FP32 rates computed from these are effective rates."""
     nr, na, P = nb["n_r"], nb["n_a"], nb["P"]
     fwd = nr * (16 + (5 + 2 * (m - 1)) * R) + 6 * na + P * (9 + (5 + 2 * (m - 1)) * A) + 2 * nsf
     adj = nr * (12 + (9 + 2 * (m - 1)) * R) + P * (77 + (8 + 2 * (m - 1)) * A)
@@ -371,10 +373,13 @@ def run_gb300(args):
     dom = max(kernels, key=lambda k: stages.get(k, 0.0))
     cap = nb["cap"]
     # algorithmic bytes per atom of each kernel (neighbour table at 20 B per
-    # pair: float4 vector + packed index; descriptor rows 4 B per feature)
+    # pair: float4 vector + packed index; descriptor rows 4 B per feature;
+    # moment rows written by the forward and read by the adjoint)
     nsf = sp["nsf"]
-    nbytes = {"descriptor": nb["n_r"] * 20 + nsf * 4,
-              "adjoint": nb["n_r"] * 20 + nsf * 4 + 16 * (nb["n_r"] + 1),
+    # moment rows of the FP32 moment form (both blocks, padded to float4)
+    mom = 4 * ((2 * A * A + 3) & ~3) if (args.angular_terms == "moments" and A <= 7) else 0
+    nbytes = {"descriptor": nb["n_r"] * 20 + nsf * 4 + mom,
+              "adjoint": nb["n_r"] * 20 + nsf * 4 + 16 * (nb["n_r"] + 1) + mom,
               "networks": 2 * nsf * 4 + 8,
               "neighbours": 24 + nb["n_r"] * 20 + 16 * 27}
     dom_ms = stages[dom]
