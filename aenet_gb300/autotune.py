@@ -1,8 +1,8 @@
 """Measured choice of the evaluator's launch shapes.
 
 Four knobs decide most of the run time of a batch: the neighbour-search
-kernel (one warp per atom, or per home cell with a lane per home atom or a
-lane per candidate), the number of neighbour-search cells per cut-off
+kernel (one warp per atom over the full or the half stencil, or per home
+cell with a lane per home atom or a lane per candidate), the number of neighbour-search cells per cut-off
 length (1, 2 or 3), their refinement along the third axis (1, 2 or 4) and
 the number of lanes that cooperate on one atom in the descriptor and
 adjoint kernels (8, 16 or 32).  The first three only change the neighbour
@@ -23,7 +23,7 @@ from .plan import Plan
 LANES = (8, 16, 32)
 CELL_DIVS = (1, 2, 3)
 Z_REFINES = (1, 2, 4)
-NB_KERNELS = ("cell", "atom", "stream")
+NB_KERNELS = ("cell", "atom", "stream", "half")
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "aenet_gb300", "autotune.json")
 
 

@@ -271,7 +271,8 @@ struct State {
   int lpa_adjoint = 0;        // lanes per atom of the adjoint (0: as the forward)
   int networks_tc = 1;       // tensor-core networks on the mixed path when eligible
   int nb_cell = 0;           // neighbour search: warp per atom (0), per home cell with a lane
-                             // per home atom (1) or per home cell with a lane per candidate (2)
+                             // per home atom (1), per home cell with a lane per candidate (2),
+                             // warp per atom over the half stencil (3)
   int angular_moments = 1;   // FP32 angular terms in moment form where instantiated
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
@@ -1923,6 +1924,7 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
   if (k == "neighbour_kernel") {
     if (v == "cell") g.nb_cell = 1;
     else if (v == "stream") g.nb_cell = 2;
+    else if (v == "half") g.nb_cell = 3;
     else if (v == "atom") g.nb_cell = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;

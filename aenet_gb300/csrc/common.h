@@ -205,7 +205,8 @@ struct NbBuffers {
   int* nb_img;                // optional: image T packed 3 x 10-bit signed
   unsigned* status;
   int cell_kernel;            // 0: warp per atom; warp per home cell with a lane per
-                              // home atom (1) or a lane per candidate (2)
+                              // home atom (1) or a lane per candidate (2); 3: warp per
+                              // atom over the half stencil, each pair written to both rows
 };
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types,

@@ -893,6 +893,227 @@ __global__ void __launch_bounds__(32 * NBS_WARPS) k_neighbors_stream(int ncells,
   }
 }
 
+// ---- half-stencil search: every pair once.  One warp per atom as in
+// k_neighbors, but only over the stencil units whose unwrapped cell offset
+// D = (d0, d1, dz) is lexicographically positive (d0 > 0; d0 = 0 and
+// d1 > 0; d0 = d1 = 0 and dz >= 0), and within the atom's own cell at T = 0
+// only partners j > i.  The offset of a pair seen from j is -D, so each
+// unordered pair (i, j, T) is met exactly once; the finder writes it to
+// both rows, (j, T) into row i and (i, -T) into row j, each side accepted
+// by its own FP64 predicate in the band.  Slots come from atomic counters
+// (nb_cnt zeroed before, clamped after): rows hold the same sets as the
+// full search in an order that depends on timing.
+constexpr int AE_HOME_UNIT = 1 << 30;   // unit flag beside the packed image
+
+template <typename T4>
+__global__ void __launch_bounds__(256, 4) k_neighbors_half(int natoms, NbBuffers nb) {
+  __shared__ int su_base[8][32];
+  __shared__ float4 su_sh[8][32];
+  __shared__ int su_first[8][32];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= natoms) return;
+  const StructGeom* g = nb.geom + nb.atom_struct[i];
+  const int pbc = g->pbc;
+  const int nc0 = g->nc[0], nc1 = g->nc[1], nc2 = g->nc[2];
+  const int k0 = g->kr[0], k1 = g->kr[1], k2 = g->kr[2];
+  const int w1 = 2 * k1 + 1;
+  const int packed = nb.cell_of[i];
+  const int c0 = packed & 1023, c1 = (packed >> 10) & 1023, c2 = (packed >> 20) & 1023;
+  const int t2lo = pbc ? floor_div_r(c2 - k2, g->inv_nc[2]) : 0;
+  const int t2hi = pbc ? floor_div_r(c2 + k2, g->inv_nc[2]) : 0;
+  const int nt2 = t2hi - t2lo + 1;
+  // rows (0, 0..k1) then (1..k0, -k1..k1); the (0, 0) row from dz = 0 up
+  const int nrows = (k1 + 1) + k0 * w1;
+  const int nunits = nrows * nt2;
+  const float4 ri = nb.r_f32[i];
+  const int iti = i | (__float_as_int(ri.w) << AE_TYPE_SHIFT);
+  const float rc2_lo = g->rc2_lo, rc2_hi = g->rc2_hi;
+  const double rc2 = g->rc2;
+  const int cap = nb.cap;
+  const int* __restrict__ cstart = nb.cell_start + g->cell_off;
+  const int home_end = cstart[(c0 * nc1 + c1) * nc2 + c2 + 1];
+  const float sf0 = (float)nb.s_wrap[3 * i], sf1 = (float)nb.s_wrap[3 * i + 1],
+              sf2 = (float)nb.s_wrap[3 * i + 2];
+  const float rcf = g->rcf * 1.0001f + 1e-4f;
+  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
+  const int ortho = g->ortho;
+  const float hf0 = g->hf[0], hf1 = g->hf[1], ihf2 = g->inv_hf[2];
+  const float* __restrict__ Lf = g->Lf;
+  int* __restrict__ cnt = nb.nb_cnt;
+  const unsigned lt = (1u << lane) - 1u;
+
+  for (int ubase = 0; ubase < nunits; ubase += 32) {
+    const int u = ubase + lane;
+    int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0, home = 0;
+    float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
+    if (u < nunits) {
+      const int rr = floor_div_r(u, inv_nt2);
+      const int it2 = u - rr * nt2;
+      int d0, d1;
+      if (rr <= k1) {
+        d0 = 0;
+        d1 = rr;
+      } else {
+        const int r2 = rr - (k1 + 1);
+        const int q0 = floor_div_r(r2, inv_w1);
+        d0 = 1 + q0;
+        d1 = r2 - q0 * w1 - k1;
+      }
+      int a0 = c0 + d0, a1 = c1 + d1;
+      bool ok = true;
+      int zlo = (d0 == 0 && d1 == 0) ? c2 : c2 - k2, zhi = c2 + k2;
+      if (ortho) {
+        const float x0 = (float)a0 * inc0, x1 = (float)(a0 + 1) * inc0;
+        const float y0 = (float)a1 * inc1, y1 = (float)(a1 + 1) * inc1;
+        const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * hf0;
+        const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * hf1;
+        const float rem = rcf * rcf - gx * gx - gy * gy;
+        if (rem < 0.f) {
+          ok = false;
+        } else {
+          const float hz = sqrtf(rem) * ihf2 * 1.0001f + 1e-6f;
+          zlo = max(zlo, (int)floorf((sf2 - hz) * nc2));
+          zhi = min(zhi, (int)floorf((sf2 + hz) * nc2));
+        }
+      }
+      if (pbc) {
+        T0 = floor_div_r(a0, inc0);
+        a0 -= T0 * nc0;
+        T1 = floor_div_r(a1, inc1);
+        a1 -= T1 * nc1;
+        T2 = t2lo + it2;
+        zlo = max(zlo, T2 * nc2);
+        zhi = min(zhi, T2 * nc2 + nc2 - 1);
+      } else {
+        ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
+        zlo = max(zlo, 0);
+        zhi = min(zhi, nc2 - 1);
+      }
+      if (ok && zlo <= zhi) {
+        const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
+        beg = cstart[base + zlo];
+        len = cstart[base + zhi + 1] - beg;
+        // the home cell (T = 0) leads the (0, 0) row of image 0
+        home = (d0 == 0 && d1 == 0 && zlo == c2) ? AE_HOME_UNIT : 0;
+        const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
+        sh0 = f0 * Lf[0] + f1 * Lf[3] + f2 * Lf[6];
+        sh1 = f0 * Lf[1] + f1 * Lf[4] + f2 * Lf[7];
+        sh2 = f0 * Lf[2] + f1 * Lf[5] + f2 * Lf[8];
+      }
+    }
+    int incl = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int w = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += w;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int start = incl - len;
+    __syncwarp();
+    su_base[warp][lane] = beg - start;
+    su_sh[warp][lane] = make_float4(
+        sh0, sh1, sh2,
+        __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) | ((T2 & 1023) << 20) | home));
+    __syncwarp();
+    int carry = 0;
+    for (int qb = 0; qb < total; qb += 32) {
+      const int q = qb + lane;
+      const bool starts = len > 0 && start >= qb && start < qb + 32;
+      __syncwarp();
+      if (starts) su_first[warp][start - qb] = lane;
+      const unsigned marks = __reduce_or_sync(0xffffffffu, starts ? (1u << (start - qb)) : 0u);
+      __syncwarp();
+      const unsigned upto = marks & (0xffffffffu >> (31 - lane));
+      const int own = upto ? su_first[warp][31 - __clz(upto)] : carry;
+      carry = __shfl_sync(0xffffffffu, own, 31);
+      const float4 osh = su_sh[warp][own];
+      const int tag = __float_as_int(osh.w);
+      const int img = tag & ~AE_HOME_UNIT;
+      bool acc_i = false, acc_j = false;
+      int j = 0, tj = 0;
+      float dx = 0.f, dy = 0.f, dz = 0.f, dd2 = 0.f;
+      if (q < total) {
+        const int p = su_base[warp][own] + q;
+        const float4 rj = nb.cell_pos[p];
+        j = nb.cell_atoms[p];
+        tj = __float_as_int(rj.w);
+        // in the atom's own cell only partners after it
+        if (!(tag & AE_HOME_UNIT) || p >= home_end || j > i) {
+          dx = (rj.x - ri.x) + osh.x;
+          dy = (rj.y - ri.y) + osh.y;
+          dz = (rj.z - ri.z) + osh.z;
+          dd2 = dx * dx + dy * dy + dz * dz;
+          if (dd2 < rc2_lo) {
+            acc_i = acc_j = true;
+          } else if (dd2 <= rc2_hi) {
+            const int t0 = sext10i(img & 1023), t1 = sext10i((img >> 10) & 1023),
+                      t2 = sext10i((img >> 20) & 1023);
+            acc_i = band_accept(g, nb, pbc, i, j, t0, t1, t2, rc2);
+            acc_j = band_accept(g, nb, pbc, j, i, -t0, -t1, -t2, rc2);
+          }
+        }
+      }
+      // row i: one counter update per batch
+      const unsigned mask = __ballot_sync(0xffffffffu, acc_i);
+      int base_i = 0;
+      if (mask) {
+        if (lane == 0) base_i = atomicAdd(cnt + i, __popc(mask));
+        base_i = __shfl_sync(0xffffffffu, base_i, 0);
+      }
+      const int nimg = ((-sext10i(img & 1023)) & 1023) |
+                       (((-sext10i((img >> 10) & 1023)) & 1023) << 10) |
+                       (((-sext10i((img >> 20) & 1023)) & 1023) << 20);
+      if (acc_i) {
+        const int k = base_i + __popc(mask & lt);
+        if (k < cap) {
+          const size_t row = (size_t)i * cap;
+          nb.nb_jt[row + k] = j | (tj << AE_TYPE_SHIFT);
+          if (nb.nb_img) nb.nb_img[row + k] = img;
+          if (VecOut<T4>::fp64) {
+            reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] = fp64_pair_vector(
+                g, nb, pbc, i, j, sext10i(img & 1023), sext10i((img >> 10) & 1023),
+                sext10i((img >> 20) & 1023));
+          } else {
+            reinterpret_cast<float4*>(nb.nb_vec)[row + k] =
+                make_float4(dx, dy, dz, pair_length(dd2));
+          }
+        }
+      }
+      // row j: the mirrored pair
+      if (acc_j) {
+        const int k = atomicAdd(cnt + j, 1);
+        if (k < cap) {
+          const size_t row = (size_t)j * cap;
+          nb.nb_jt[row + k] = iti;
+          if (nb.nb_img) nb.nb_img[row + k] = nimg;
+          if (VecOut<T4>::fp64) {
+            reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] = fp64_pair_vector(
+                g, nb, pbc, j, i, -sext10i(img & 1023), -sext10i((img >> 10) & 1023),
+                -sext10i((img >> 20) & 1023));
+          } else {
+            reinterpret_cast<float4*>(nb.nb_vec)[row + k] =
+                make_float4(-dx, -dy, -dz, pair_length(dd2));
+          }
+        }
+      }
+    }
+  }
+}
+
+// counts of the half-stencil search: clamp to the capacity, flag overflow
+__global__ void k_clamp_counts(int natoms, int cap, int* __restrict__ cnt, unsigned* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  const int c = cnt[i];
+  if (c > cap) {
+    cnt[i] = cap;
+    atomicOr(status, AE_ST_NB_OVERFLOW);
+  }
+}
+
 // ---- caller's neighbour list (CSR over local atoms, indices into local +
 // ghost atoms) -> ELL table.  R_ij = x_j - x_i in FP64; pairs beyond
 // (Rc + 1e-3) are dropped; species from the caller's type ids.
@@ -981,6 +1202,17 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
   k_scan_sums<<<1, SCAN_B, 0, s>>>(nblk, nb.scan_tmp, nb.cell_start + nc);
   k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
   k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
+  if (nb.cell_kernel == 3) {
+    e = cudaMemsetAsync(nb.nb_cnt, 0, sizeof(int) * (size_t)natoms, s);
+    if (e != cudaSuccess) return (int)e;
+    const int blocks = (natoms + 7) / 8;
+    if (fp64)
+      k_neighbors_half<double4_32a><<<blocks, 256, 0, s>>>(natoms, nb);
+    else
+      k_neighbors_half<float4><<<blocks, 256, 0, s>>>(natoms, nb);
+    k_clamp_counts<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb.cap, nb.nb_cnt, nb.status);
+    return (int)cudaGetLastError();
+  }
   if (nb.cell_kernel == 2) {
     const int blocks = (nc + NBS_WARPS - 1) / NBS_WARPS;
     if (fp64)

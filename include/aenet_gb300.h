@@ -46,12 +46,14 @@ extern "C" {
  *       finely to the cut-off sphere (performance only).
  *   "lanes_per_atom" = "8" | "16" | "32"   descriptor kernels' lanes per
  *       atom (performance only).
- *   "neighbour_kernel" = "atom" | "cell" | "stream"   neighbour search
- *       with one warp per atom (pruned per atom), one warp per home cell
- *       with a lane per home atom (dense cells of large structures) or one
- *       warp per home cell with a lane per candidate, each batch of
- *       candidates tested against every home atom (few atoms per cell);
- *       same neighbour sets (performance only).
+ *   "neighbour_kernel" = "atom" | "cell" | "stream" | "half"   neighbour
+ *       search with one warp per atom (pruned per atom), one warp per home
+ *       cell with a lane per home atom (dense cells of large structures),
+ *       one warp per home cell with a lane per candidate, each batch of
+ *       candidates tested against every home atom (few atoms per cell), or
+ *       one warp per atom over half the stencil, each pair found once and
+ *       written to both rows (the order inside a row then varies from run
+ *       to run); same neighbour sets (performance only).
  *   "networks" = "tensor" | "simt"   mixed-path networks on the tcgen05
  *       tensor cores (split BF16, FP32 accumulation; networks with two
  *       hidden layers and widths up to 64) or on FP32 SIMT.

@@ -49,12 +49,12 @@ def aucu(oracle, tmp_path_factory):
     return w, paths
 
 
-@pytest.fixture(params=["atom", "cell", "stream", "atom_z4", "stream_z2"])
+@pytest.fixture(params=["atom", "cell", "stream", "half", "atom_z4", "stream_z2", "half_z4"])
 def nb_kernel(request, cuda):
-    """Run a test with each neighbour-search kernel (one warp per atom, or
-    one warp per home cell with a lane per home atom or per candidate),
-    also on grids refined along the third axis; restores the defaults
-    afterwards."""
+    """Run a test with each neighbour-search kernel (one warp per atom over
+    the full or the half stencil, or one warp per home cell with a lane per
+    home atom or per candidate), also on grids refined along the third
+    axis; restores the defaults afterwards."""
     from aenet_gb300.core import set_option
     kernel, _, z = request.param.partition("_z")
     set_option("neighbour_kernel", kernel)
