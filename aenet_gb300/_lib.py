@@ -106,6 +106,10 @@ def _declare(lib):
     lib.aenet_gpu_save_potential.restype = C.c_int
     lib.aenet_gpu_plan_load_descriptors.argtypes = [vp, vp, C.c_int]
     lib.aenet_gpu_plan_load_descriptors.restype = C.c_int
+    lib.aenet_gpu_plan_neighbour_capacity.argtypes = [vp]
+    lib.aenet_gpu_plan_neighbour_capacity.restype = C.c_int
+    lib.aenet_gpu_plan_descriptor_jacobian.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp]
+    lib.aenet_gpu_plan_descriptor_jacobian.restype = C.c_int
     lib.aenet_gpu_plan_descriptor_loss_gradient.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     lib.aenet_gpu_plan_descriptor_loss_gradient.restype = C.c_int
     lib.aenet_gpu_neighbor_list_energy_forces.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, C.c_int,

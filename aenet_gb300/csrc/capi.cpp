@@ -2512,6 +2512,25 @@ EXPORT int aenet_gpu_plan_load_descriptors(aenet_gpu_plan* P, const double* G, i
   return AENET_OK;
 }
 
+// Descriptor Jacobians (raw, FP64) of atoms [atom0, atom0 + count) from the
+// neighbour table of the plan's last run: generate.x's PyTorch export.
+EXPORT int aenet_gpu_plan_neighbour_capacity(const aenet_gpu_plan* P) { return P ? P->cap : -1; }
+
+EXPORT int aenet_gpu_plan_descriptor_jacobian(aenet_gpu_plan* P, int atom0, int count,
+                                              double* d_dG_i, double* d_dG_j, int* d_nbl,
+                                              int* d_nnb, void* stream) {
+  if (!P || !P->pd || !P->fp64 || !d_dG_i || !d_dG_j || !d_nbl || !d_nnb) return AENET_ERR_INPUT;
+  if (atom0 < 0 || count < 0 || atom0 + count > P->natoms) return AENET_ERR_INPUT;
+  const PotDevice& pd = *P->pd;
+  for (int t = 0; t < pd.ntypes; ++t)
+    if (pd.sp[t].sftype != AE_SF_CHEBYSHEV) return AENET_ERR_INPUT;
+  DescBuffers d = desc_buffers(P, nullptr, false);
+  if (ck(ae_launch_chebyshev_jacobian(pd, d, atom0, count, pd.nsf_max, d_dG_i, d_dG_j, d_nbl,
+                                      d_nnb, (cudaStream_t)stream)))
+    return AENET_ERR_CUDA;
+  return AENET_OK;
+}
+
 // The reference's energy loss and weight gradient from the loaded
 // descriptors (no positions, no neighbour search): networks, per-structure
 // energies, SSE = sum_s dE_s^2/2 and sum_s dE_s Dw_s.

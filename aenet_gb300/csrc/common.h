@@ -246,6 +246,13 @@ int ae_launch_chebyshev_adjoint(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);
 int ae_launch_chebyshev_tangent(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);
+// FP64 descriptor Jacobians of atoms [atom0, atom0 + count): dG/dR of the
+// central atom [count][nsf_max][3] and of every neighbour slot
+// [count][cap][nsf_max][3], the neighbours' atom indices [count][cap] and
+// counts [count]
+int ae_launch_chebyshev_jacobian(const PotDevice& pd, const DescBuffers& b, int atom0, int count,
+                                 int nsf_max, double* Ji, double* Jj, int* nbl, int* nnb,
+                                 cudaStream_t s);
 int ae_launch_behler_forward(const PotDevice& pd, const DescBuffers& b,
                              int fp64, cudaStream_t s);
 int ae_launch_behler_adjoint(const PotDevice& pd, const DescBuffers& b,

@@ -10,6 +10,10 @@ generate.x leaves them for train.x's normalisation.
 
 The descriptors come from the GPU FP64 path: the potentials are loaded with
 identity normalisation, so the plan's descriptor rows are the raw values.
+With ``forces_percent`` the descriptor Jacobians of that share of the
+structures are written beside the training set in the PyTorch export
+format of generate.x's FORCES keyword (aenet_gb300/pytorch_export.py,
+Chebyshev bases).
 """
 import os
 import tempfile
@@ -20,17 +24,20 @@ import torch
 from . import nnfile
 from .core import ANNPotentials, FP64
 from .plan import Plan
+from .pytorch_export import select_structures, write_forces_file
 from .trainset import TrainSet, write_trainset
 from .workloads import running_stats
 
 __all__ = ["generate_trainset"]
 
 
-def generate_trainset(potential_files, structures, path):
+def generate_trainset(potential_files, structures, path, forces_percent=None, seed=0):
     """``potential_files``: species -> .nn (their setups define the
     descriptors); ``structures``: dicts with positions, symbols, cell (None
     for isolated), energy (total, eV), optional forces and name.  Writes
-    ``path`` and returns the TrainSet."""
+    ``path`` and returns the TrainSet.  ``forces_percent`` (the FORCESPERCENT
+    keyword, 0-100) also writes ``path + ".forces"`` with the descriptor
+    Jacobians of that share of the structures (chosen with ``seed``)."""
     types = list(potential_files.keys())
     setups, E_atom = {}, {}
     tmp = tempfile.mkdtemp(prefix="aenet_generate_")
@@ -61,6 +68,9 @@ def generate_trainset(potential_files, structures, path):
         out = plan.run(p, t, forces=False)
         plan.check()
         G = plan.descriptors().cpu().numpy()
+        if forces_percent is not None:
+            _write_jacobians(plan, structures, natoms, tid, len(types), setups, types,
+                             path + ".forces", forces_percent / 100.0, seed)
         plan.close()
     finally:
         ann.release()
@@ -89,3 +99,27 @@ def generate_trainset(potential_files, structures, path):
         ts.setup_records.append(nnfile.setup_payloads(stp, legacy=legacy))
     write_trainset(path, ts)
     return ts
+
+
+def _write_jacobians(plan, structures, natoms, tid, ntypes, setups, types, path, fraction, seed):
+    """Jacobians of the selected structures from the plan's last run, one
+    structure at a time, in the PyTorch export format."""
+    flags = select_structures(len(structures), fraction, seed)
+    recs = []
+    row = 0
+    for k, s in enumerate(structures):
+        n = natoms[k]
+        rec = {"name": s.get("name", "structure-%d" % (k + 1)), "natoms": n, "ntypes": ntypes,
+               "selected": bool(flags[k]), "atoms": []}
+        if flags[k]:
+            Ji, Jj, nbl, nnb = plan.jacobian(row, n)
+            Ji, Jj, nbl, nnb = (x.cpu().numpy() for x in (Ji, Jj, nbl, nnb))
+            for a in range(n):
+                it = int(tid[row + a])
+                nsf = setups[types[it - 1]]["nsf"]
+                m = int(nnb[a])
+                rec["atoms"].append((it, nbl[a, :m] - row + 1, Ji[a, :nsf],
+                                     Jj[a, :m, :nsf]))
+        recs.append(rec)
+        row += n
+    write_forces_file(path, recs)

@@ -218,6 +218,26 @@ class Plan:
         vec = torch.as_tensor(_DeviceArray(pv.value, (n, c, 4), vt), device="cuda")
         return c, cnt, jt, vec
 
+    def jacobian(self, atom0=0, count=None, nsf_max=None):
+        """Raw FP64 descriptor Jacobians of atoms [atom0, atom0 + count) from
+        the neighbour table of the last run (Chebyshev bases, FP64 plans):
+        (dG/dR_i [count, nsf_max, 3], dG/dR_j [count, cap, nsf_max, 3],
+        neighbour atom indices [count, cap], neighbour counts [count]) as
+        CUDA tensors (aenet_gpu_plan_descriptor_jacobian)."""
+        lib = _lib.lib()
+        count = self.natoms - atom0 if count is None else count
+        if nsf_max is None:
+            nsf_max = C.c_int.in_dll(lib, "aenet_nsf_max").value
+        cap = lib.aenet_gpu_plan_neighbour_capacity(self._h)
+        dev = torch.device("cuda")
+        Ji = torch.empty((count, nsf_max, 3), dtype=torch.float64, device=dev)
+        Jj = torch.empty((count, cap, nsf_max, 3), dtype=torch.float64, device=dev)
+        nbl = torch.empty((count, cap), dtype=torch.int32, device=dev)
+        nnb = torch.empty((count,), dtype=torch.int32, device=dev)
+        check_status(lib.aenet_gpu_plan_descriptor_jacobian(self._h, int(atom0), int(count), _p(Ji),
+                                                            _p(Jj), _p(nbl), _p(nnb), _stream()))
+        return Ji, Jj, nbl, nnb
+
     def descriptors(self):
         pg = C.c_void_p()
         pad = C.c_int(0)

@@ -196,6 +196,22 @@ int aenet_gpu_plan_loss_gradient(aenet_gpu_plan* plan, const double* d_coords,
  * (AENET_GPU_LOSS_ENERGY semantics; d_E_target are total energies in eV)
  * without positions or a neighbour search. */
 int aenet_gpu_plan_load_descriptors(aenet_gpu_plan* plan, const double* G, int ld);
+
+/* Descriptor Jacobians for generate.x's PyTorch export (sfderiv_i and
+ * sfderiv_j of stp_eval, written by pyo_write_atom_sf_info,
+ * src/pytorchoutput.f90:104-138): raw (unnormalised) FP64 derivatives of
+ * the Chebyshev descriptors of atoms [atom0, atom0 + count) with respect to
+ * the central atom, d_dG_i[count][nsf_max][3], and to each neighbour slot,
+ * d_dG_j[count][cap][nsf_max][3]; d_nbl[count][cap] the neighbours' 0-based
+ * atom indices in the batch (periodic images repeat an index), d_nnb[count]
+ * the neighbour counts.  Reads the neighbour table of the plan's last run
+ * (aenet_gpu_plan_run or _forward), so call it after one; FP64 plans and
+ * Chebyshev bases only (AENET_ERR_INPUT otherwise).  nsf_max is
+ * aenet_nsf_max, cap the value of aenet_gpu_plan_neighbour_capacity. */
+int aenet_gpu_plan_neighbour_capacity(const aenet_gpu_plan* plan);
+int aenet_gpu_plan_descriptor_jacobian(aenet_gpu_plan* plan, int atom0, int count,
+                                       double* d_dG_i, double* d_dG_j, int* d_nbl,
+                                       int* d_nnb, void* stream);
 int aenet_gpu_plan_descriptor_loss_gradient(aenet_gpu_plan* plan, const int* d_types,
                                             const double* d_E_target, double* d_loss,
                                             double* d_grad, double* d_E, void* stream);

@@ -232,3 +232,69 @@ def test_generate_and_train_from_trainset_file(cuda, oracle, batch, tmp_path):
         ann.release()
     assert abs(l1 - l0) <= 1e-9 * l0
     assert np.abs(g1 - g0).max() <= 1e-9 * np.abs(g0).max()
+
+
+def test_descriptor_jacobians_match_oracle_and_export_file(cuda, oracle, batch, tmp_path):
+    """generate.x's PyTorch export: the FP64 descriptor Jacobians of every
+    neighbour slot and of the central atom against the oracle's stp_eval
+    derivatives (sfb_radial / sfb_angular restated), matched by pair
+    vector; then the .forces file written by generate_trainset holds the
+    same numbers in the reference's record layout."""
+    import torch
+    from aenet_gb300.core import FP64
+    from aenet_gb300.generate import generate_trainset
+    from aenet_gb300.plan import Plan
+    from aenet_gb300.pytorch_export import read_forces_file
+    w, paths, tpaths = batch
+    oracle.load(w.types, paths)
+    ann = _ann(paths, w.types)
+    try:
+        for s in w.structures[:3]:
+            plan = Plan([s.natoms], s.cell[None], np.array([1], dtype=np.int32), precision=FP64)
+            p = torch.tensor(s.positions, device="cuda")
+            t = torch.tensor(s.types.astype(np.int32), device="cuda")
+            plan.run(p, t, forces=False)
+            plan.check()
+            Ji, Jj, nbl, nnb = (x.cpu().numpy() for x in plan.jacobian())
+            _, _, _, vec = plan.neighbors()
+            vec = vec.cpu().numpy()
+            plan.close()
+            _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types)
+            for a in range(s.natoms):
+                nbcoo, _, nblist, nbt = nb[a]
+                G, di, dj = oracle.descriptor(centres[a], int(s.types[a]), nbcoo, nbt,
+                                              scaled=False, deriv=True)
+                nsf = G.size
+                m = int(nnb[a])
+                assert m == len(nblist)
+                scale = max(1.0, np.abs(dj).max())
+                np.testing.assert_allclose(Ji[a, :nsf], di, rtol=0, atol=1e-9 * scale)
+                R_ref = nbcoo - centres[a]
+                for q in range(m):
+                    k = int(np.argmin(np.abs(R_ref - vec[a, q, :3]).sum(1)))
+                    assert np.abs(R_ref[k] - vec[a, q, :3]).max() < 1e-9
+                    assert nbl[a, q] + 1 == nblist[k]
+                    np.testing.assert_allclose(Jj[a, q, :nsf], dj[k], rtol=0, atol=1e-9 * scale)
+    finally:
+        ann.release()
+    # generate_trainset loads its own (identity-normalised) potentials
+    structs = [{"positions": s.positions, "symbols": [w.types[t - 1] for t in s.types],
+                "cell": s.cell, "energy": -1.0, "name": "s%d" % k}
+               for k, s in enumerate(w.structures[:4])]
+    generate_trainset({t: paths[t] for t in w.types}, structs, str(tmp_path / "set.train"),
+                      forces_percent=50.0, seed=3)
+    recs, max_nnb = read_forces_file(str(tmp_path / "set.train.forces"))
+    assert len(recs) == 4 and sum(r["selected"] for r in recs) == 2
+    seen = 0
+    for k, r in enumerate(recs):
+        s = w.structures[k]
+        assert r["name"] == "s%d" % k and r["natoms"] == s.natoms and r["ntypes"] == 3
+        if not r["selected"]:
+            assert r["atoms"] == []
+            continue
+        for a, (itype, nbl1, dGi, dGj) in enumerate(r["atoms"]):
+            assert itype == s.types[a]
+            assert nbl1.min() >= 1 and nbl1.max() <= s.natoms
+            np.testing.assert_allclose(dGi, -dGj.sum(0), rtol=0, atol=1e-9 * max(1, np.abs(dGj).max()))
+            seen = max(seen, len(nbl1))
+    assert max_nnb == seen
