@@ -7,11 +7,14 @@ L-BFGS-B step over the flattened weights of all species.  Here the loss and
 gradient of the whole training set come from one GPU pass
 (``aenet_gpu_plan_loss_gradient``: neighbours, descriptors, networks,
 forces, descriptor tangents and weight gradients), and the optimiser is
-L-BFGS-B with m = 20 correction pairs and no bounds, as opt_init_bfgs sets
-it up (src/optimize.f90:1600-1609).  The reference links L-BFGS-B 3.0
-(lib/Lbfgsb.3.0, Byrd, Lu, Nocedal and Zhu); scipy.optimize ships an
-implementation of the same algorithm, used here on the host -- it handles a
-vector of a few thousand weights per step, negligible next to the GPU pass.
+L-BFGS with m = 20 correction pairs and no bounds, as opt_init_bfgs sets
+up L-BFGS-B (src/optimize.f90:1600-1609), one iteration per epoch.  The
+optimiser (aenet_gb300/lbfgs.py) runs on the host -- a vector of a few
+thousand weights per step, negligible next to the GPU pass -- and saves
+its state to a restart file after each epoch when asked, as train.x saves
+`train.restart`; a run started with an existing restart file resumes from
+it.  scipy's L-BFGS-B (the same algorithm as the reference's library) is
+available as ``optimizer="scipy"``, without restarts.
 
 Two losses (``mode``):
   LOSS_ENERGY         the reference's: sum_s dE_s^2/2 with
@@ -19,29 +22,65 @@ Two losses (``mode``):
   LOSS_ENERGY_FORCES  w_E sum_s (E_s - E_t,s)^2/N_s^2 + w_F sum_i |F_i - F_t,i|^2.
 """
 import ctypes as C
+import os
+from types import SimpleNamespace
 
 import numpy as np
 import torch
 
 from . import _lib
 from .core import FP64, check_status
+from .lbfgs import LBFGS
 from .plan import LOSS_ENERGY, LOSS_ENERGY_FORCES, Plan, _p, _stream
 
 __all__ = ["Trainer", "DescriptorTrainer", "LOSS_ENERGY", "LOSS_ENERGY_FORCES"]
 
 
 class _Fit:
-    """L-BFGS-B over all weights (opt_bfgs_weights, src/optimize.f90:1721-1771)."""
+    """L-BFGS over all weights (opt_bfgs_weights, src/optimize.f90:1721-1771)."""
 
-    def fit(self, maxiter=100, m=20, gtol=0.0, ftol=0.0, callback=None):
-        """Leaves the final weights loaded and returns scipy's OptimizeResult."""
-        from scipy.optimize import minimize
-        x0 = self.pot.get_weights()
-        res = minimize(self.loss_and_grad, x0, jac=True, method="L-BFGS-B", callback=callback,
-                       options={"maxcor": int(m), "maxiter": int(maxiter), "gtol": gtol,
-                                "ftol": ftol})
-        self.pot.set_weights(res.x)
-        return res
+    def fit(self, maxiter=100, m=20, gtol=0.0, ftol=0.0, callback=None, restart=None,
+            save_every=1, optimizer="lbfgs"):
+        """``maxiter`` iterations (epochs) at most; stops early when the
+        largest gradient component is at most ``gtol`` or the relative
+        decrease of one iteration is at most ``ftol``.  ``restart``: path of
+        the optimiser's state, resumed from when the file exists and written
+        every ``save_every`` iterations.  Leaves the final weights loaded and
+        returns (x, fun, jac, nit, nfev, success, message)."""
+        if optimizer == "scipy":
+            from scipy.optimize import minimize
+            x0 = self.pot.get_weights()
+            res = minimize(self.loss_and_grad, x0, jac=True, method="L-BFGS-B",
+                           callback=callback, options={"maxcor": int(m), "maxiter": int(maxiter),
+                                                       "gtol": gtol, "ftol": ftol})
+            self.pot.set_weights(res.x)
+            return res
+        if restart is not None and os.path.exists(restart):
+            opt = LBFGS.load(self.loss_and_grad, restart, m=m)
+        else:
+            opt = LBFGS(self.loss_and_grad, self.pot.get_weights(), m=m)
+        message = "maximum number of iterations"
+        success = True
+        for _ in range(int(maxiter)):
+            if np.abs(opt.g).max() <= gtol:
+                message = "gradient below gtol"
+                break
+            f_old = opt.f
+            if not opt.step():
+                message, success = "no decrease along the search direction", False
+                break
+            if callback is not None:
+                callback(opt.x)
+            if restart is not None and opt.k % max(1, int(save_every)) == 0:
+                opt.save(restart)
+            if ftol and f_old - opt.f <= ftol * max(abs(f_old), abs(opt.f), 1.0):
+                message = "relative decrease below ftol"
+                break
+        if restart is not None:
+            opt.save(restart)
+        self.pot.set_weights(opt.x)
+        return SimpleNamespace(x=opt.x, fun=opt.f, jac=opt.g, nit=opt.k, nfev=opt.nfev,
+                               success=success, message=message)
 
 
 class Trainer(_Fit):

@@ -298,3 +298,28 @@ def test_descriptor_jacobians_match_oracle_and_export_file(cuda, oracle, batch, 
             np.testing.assert_allclose(dGi, -dGj.sum(0), rtol=0, atol=1e-9 * max(1, np.abs(dGj).max()))
             seen = max(seen, len(nbl1))
     assert max_nnb == seen
+
+
+def test_fit_resumes_from_restart_file(cuda, batch, tmp_path):
+    """train.restart semantics: 3 + 3 iterations through the restart file
+    reach the weights of 6 uninterrupted iterations (FP64 energy loss)."""
+    from aenet_gb300.core import FP64
+    from aenet_gb300.train import LOSS_ENERGY, Trainer
+    w, paths, tpaths = batch
+    E_t, _ = _targets(w, tpaths)
+    ann = _ann(paths, w.types)
+    try:
+        W0 = ann.get_weights()
+        tr = Trainer(ann, _structs(w), E_t, mode=LOSS_ENERGY, precision=FP64)
+        r6 = tr.fit(maxiter=6)
+        ann.set_weights(W0)
+        path = str(tmp_path / "train.restart")
+        r3 = tr.fit(maxiter=3, restart=path)
+        ann.set_weights(W0 * 0.0)     # the restart file, not the loaded weights, decides
+        r33 = tr.fit(maxiter=3, restart=path)
+        tr.close()
+    finally:
+        ann.release()
+    assert r3.nit == 3 and r33.nit == 6 and r6.nit == 6
+    assert abs(r33.fun - r6.fun) <= 1e-9 * abs(r6.fun)
+    np.testing.assert_allclose(r33.x, r6.x, rtol=0, atol=1e-8 * np.abs(r6.x).max())
