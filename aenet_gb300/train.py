@@ -40,13 +40,15 @@ class _Fit:
     """L-BFGS over all weights (opt_bfgs_weights, src/optimize.f90:1721-1771)."""
 
     def fit(self, maxiter=100, m=20, gtol=0.0, ftol=0.0, callback=None, restart=None,
-            save_every=1, optimizer="lbfgs"):
+            save_every=1, optimizer="lbfgs", nn_files=None):
         """``maxiter`` iterations (epochs) at most; stops early when the
         largest gradient component is at most ``gtol`` or the relative
         decrease of one iteration is at most ``ftol``.  ``restart``: path of
         the optimiser's state, resumed from when the file exists and written
-        every ``save_every`` iterations.  Leaves the final weights loaded and
-        returns (x, fun, jac, nit, nfev, success, message)."""
+        every ``save_every`` iterations; ``nn_files`` (species -> path): the
+        potentials written at the same times and at the end, as train.x
+        writes its .nn files.  Leaves the final weights loaded and returns
+        (x, fun, jac, nit, nfev, success, message)."""
         if optimizer == "scipy":
             from scipy.optimize import minimize
             x0 = self.pot.get_weights()
@@ -71,16 +73,27 @@ class _Fit:
                 break
             if callback is not None:
                 callback(opt.x)
-            if restart is not None and opt.k % max(1, int(save_every)) == 0:
-                opt.save(restart)
+            if opt.k % max(1, int(save_every)) == 0:
+                if restart is not None:
+                    opt.save(restart)
+                self._save_nn(nn_files, opt.x)
             if ftol and f_old - opt.f <= ftol * max(abs(f_old), abs(opt.f), 1.0):
                 message = "relative decrease below ftol"
                 break
         if restart is not None:
             opt.save(restart)
         self.pot.set_weights(opt.x)
+        self._save_nn(nn_files, opt.x)
         return SimpleNamespace(x=opt.x, fun=opt.f, jac=opt.g, nit=opt.k, nfev=opt.nfev,
                                success=success, message=message)
+
+
+    def _save_nn(self, nn_files, x):
+        if not nn_files:
+            return
+        self.pot.set_weights(x)
+        for name, path in nn_files.items():
+            self.pot.save_potential(name, path)
 
 
 class Trainer(_Fit):

@@ -314,12 +314,15 @@ def test_fit_resumes_from_restart_file(cuda, batch, tmp_path):
         r6 = tr.fit(maxiter=6)
         ann.set_weights(W0)
         path = str(tmp_path / "train.restart")
-        r3 = tr.fit(maxiter=3, restart=path)
+        r3 = tr.fit(maxiter=3, restart=path, nn_files={w.types[0]: str(tmp_path / "a.nn")})
         ann.set_weights(W0 * 0.0)     # the restart file, not the loaded weights, decides
         r33 = tr.fit(maxiter=3, restart=path)
         tr.close()
     finally:
         ann.release()
     assert r3.nit == 3 and r33.nit == 6 and r6.nit == 6
+    from aenet_gb300.nnfile import read_nn
+    net, _, _, _ = read_nn(str(tmp_path / "a.nn"))
+    assert np.array_equal(net["W"], r3.x[:net["W"].size])
     assert abs(r33.fun - r6.fun) <= 1e-9 * abs(r6.fun)
     np.testing.assert_allclose(r33.x, r6.x, rtol=0, atol=1e-8 * np.abs(r6.x).max())
