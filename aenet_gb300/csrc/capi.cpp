@@ -854,6 +854,7 @@ struct aenet_gpu_plan {
   unsigned* status = nullptr;
   int nchunks = 0;            // energy-reduction chunks over all structures
   double2* e_part = nullptr;
+  int* chunk_struct = nullptr;  // [nchunks] structure of each energy chunk
   int* order = nullptr;       // atoms grouped by species (tensor-core networks, training)
   int* spec_off = nullptr;    // [AE_MAXT + 1]
   int* part_scratch = nullptr;
@@ -1097,6 +1098,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_V = take(72 * (size_t)P->nstruc);
   size_t o_st = take(16);
   size_t o_ep = take(16 * (size_t)(P->nchunks + 1));
+  size_t o_chs = take(4 * (size_t)(P->nchunks + 1));
   size_t o_ord = take(4 * (size_t)N);
   size_t o_spo = take(4 * (AE_MAXT + 1));
   size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(N));
@@ -1129,6 +1131,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->virial = (double*)(b + o_V);
   P->status = (unsigned*)(b + o_st);
   P->e_part = (double2*)(b + o_ep);
+  P->chunk_struct = (int*)(b + o_chs);
   P->order = (int*)(b + o_ord);
   P->spec_off = (int*)(b + o_spo);
   P->part_scratch = (int*)(b + o_ps);
@@ -1137,6 +1140,12 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
     for (int q = 0; q < P->natoms_h[s]; ++q) as[a++] = s;
   cudaMemcpy(P->geom_d, P->geom_h.data(), sizeof(StructGeom) * P->nstruc, cudaMemcpyHostToDevice);
   if (N) cudaMemcpy(P->atom_struct, as.data(), 4 * (size_t)N, cudaMemcpyHostToDevice);
+  std::vector<int> cs;
+  cs.reserve(P->nchunks);
+  for (int s = 0; s < P->nstruc; ++s)
+    for (int c = 0; c < (P->natoms_h[s] + AE_ECHUNK - 1) / AE_ECHUNK; ++c) cs.push_back(s);
+  if (!cs.empty())
+    cudaMemcpy(P->chunk_struct, cs.data(), 4 * cs.size(), cudaMemcpyHostToDevice);
   cudaMemset(P->status, 0, 16);
   if (cudaDeviceSynchronize() != cudaSuccess) return AENET_ERR_CUDA;
   return 0;
@@ -1260,8 +1269,8 @@ int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s)
                                              : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
   if (ck(e)) return AENET_ERR_CUDA;
   if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
-  if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->E_atom, P->e_part,
-                                         P->E_struct, s)))
+  if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->chunk_struct,
+                                         P->E_atom, P->e_part, P->E_struct, s)))
     return AENET_ERR_CUDA;
   if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
     return AENET_ERR_CUDA;
@@ -2548,8 +2557,8 @@ EXPORT int aenet_gpu_plan_descriptor_loss_gradient(aenet_gpu_plan* P, const int*
   if (ck(ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s))) return AENET_ERR_CUDA;
   DescBuffers d = desc_buffers(P, nullptr, false);
   if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
-  if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->E_atom, P->e_part,
-                                         P->E_struct, s)))
+  if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->chunk_struct,
+                                         P->E_atom, P->e_part, P->E_struct, s)))
     return AENET_ERR_CUDA;
   if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
     return AENET_ERR_CUDA;
@@ -2657,8 +2666,8 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   cudaEventRecord(ev[3], s);
   e |= plan_networks(P, d, s);
   cudaEventRecord(ev[4], s);
-  e |= ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->E_atom, P->e_part,
-                                       P->E_struct, s);
+  e |= ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->chunk_struct,
+                                       P->E_atom, P->e_part, P->E_struct, s);
   if (d_E) cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s);
   cudaEventRecord(ev[5], s);
   const size_t tsz = P->fp64 ? 8 : 4;

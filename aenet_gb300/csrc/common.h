@@ -265,11 +265,12 @@ int ae_launch_mlp_tc(const PotDevice& pd, const DescBuffers& b, const int* order
 int ae_fma_peak(double* tflops, cudaStream_t s);
 int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes,
                     unsigned* status, cudaStream_t s);
-// per-structure energies of large structures: Neumaier sums over chunks of
-// AE_ECHUNK atoms (one warp each), then over each structure's chunks
+// per-structure energies: FP64 sums over chunks of AE_ECHUNK atoms (one
+// warp each; chunk_struct[c] = structure of chunk c), then over each
+// structure's chunks, in pairwise order
 int ae_launch_energy_reduce_chunked(int nstruc, int nchunks, const StructGeom* geom,
-                                    const double* E_atom, double2* part, double* E_struct,
-                                    cudaStream_t s);
+                                    const int* chunk_struct, const double* E_atom, double2* part,
+                                    double* E_struct, cudaStream_t s);
 int ae_launch_energy_reduce(int nstruc, const StructGeom* geom,
                             const double* E_atom, double* E_struct,
                             cudaStream_t s);

@@ -175,38 +175,25 @@ __global__ void k_energy_reduce(int nstruc, const StructGeom* geom, const double
 
 // chunk c of the structure whose chunk range contains it
 __global__ void k_energy_chunks(int nstruc, int nchunks, const StructGeom* __restrict__ geom,
+                                const int* __restrict__ chunk_struct,
                                 const double* __restrict__ E_atom, double2* __restrict__ part,
                                 double* __restrict__ E_struct) {
   const int lane = threadIdx.x & 31;
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (c >= nchunks) return;
-  int lo = 0, hi = nstruc - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (geom[mid].chunk_off <= c) lo = mid; else hi = mid - 1;
-  }
-  const StructGeom& g = geom[lo];
+  const int sidx = chunk_struct[c];
+  const StructGeom& g = geom[sidx];
   const int a0 = (c - g.chunk_off) * AE_ECHUNK;
   const int a1 = min(g.natoms, a0 + AE_ECHUNK);
-  double s = 0.0, e = 0.0;
-  for (int a = a0 + lane; a < a1; a += 32) {
-    double t, r;
-    two_sum(s, E_atom[g.atom_off + a], t, r);
-    s = t;
-    e += r;
-  }
+  // pairwise order (a lane's run, then a tree over the lanes): the rounding
+  // error stays within (AE_ECHUNK/32 + 5) ulp of sum |E_i|
+  double s = 0.0;
+  for (int a = a0 + lane; a < a1; a += 32) s += E_atom[g.atom_off + a];
 #pragma unroll
-  for (int d = 16; d > 0; d >>= 1) {
-    const double so = __shfl_xor_sync(0xffffffffu, s, d);
-    const double eo = __shfl_xor_sync(0xffffffffu, e, d);
-    double t, r;
-    two_sum(s, so, t, r);
-    s = t;
-    e = e + eo + r;
-  }
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
   if (lane == 0) {
-    part[c] = make_double2(s, e);
-    if (g.natoms <= AE_ECHUNK) E_struct[lo] = s + e;   // single chunk: final already
+    part[c] = make_double2(s, 0.0);
+    if (g.natoms <= AE_ECHUNK) E_struct[sidx] = s;   // single chunk: final already
   }
 }
 
@@ -223,24 +210,11 @@ __global__ void k_energy_struct(int nstruc, int nchunks, const StructGeom* __res
     if (lane == 0) E_struct[sidx] = 0.0;
     return;
   }
-  double s = 0.0, e = 0.0;
-  for (int c = c0 + lane; c < c1; c += 32) {
-    const double2 p = part[c];
-    double t, r;
-    two_sum(s, p.x, t, r);
-    s = t;
-    e += r + p.y;
-  }
+  double s = 0.0;
+  for (int c = c0 + lane; c < c1; c += 32) s += part[c].x;
 #pragma unroll
-  for (int d = 16; d > 0; d >>= 1) {
-    const double so = __shfl_xor_sync(0xffffffffu, s, d);
-    const double eo = __shfl_xor_sync(0xffffffffu, e, d);
-    double t, r;
-    two_sum(s, so, t, r);
-    s = t;
-    e = e + eo + r;
-  }
-  if (lane == 0) E_struct[sidx] = s + e;
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+  if (lane == 0) E_struct[sidx] = s;
 }
 
 template <typename T>
@@ -347,12 +321,12 @@ int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStrea
 }
 
 int ae_launch_energy_reduce_chunked(int nstruc, int nchunks, const StructGeom* geom,
-                                    const double* E_atom, double2* part, double* E_struct,
-                                    cudaStream_t s) {
+                                    const int* chunk_struct, const double* E_atom, double2* part,
+                                    double* E_struct, cudaStream_t s) {
   if (nstruc <= 0) return 0;
   if (nchunks > 0)
-    k_energy_chunks<<<(nchunks + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, E_atom, part,
-                                                      E_struct);
+    k_energy_chunks<<<(nchunks + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, chunk_struct, E_atom,
+                                                      part, E_struct);
   k_energy_struct<<<(nstruc + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, part, E_struct);
   return (int)cudaGetLastError();
 }
