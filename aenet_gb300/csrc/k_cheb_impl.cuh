@@ -67,20 +67,28 @@ __device__ __forceinline__ int warp_max(int v) {
 }
 
 // fc(d) = 0.5 (cos(pi d / Rc) + 1), fc' = -0.5 (pi/Rc) sin(pi d / Rc), zero
-// beyond Rc (sfb_fc / sfb_fc_d1, sfbasis.f90:719-752)
+// beyond Rc (sfb_fc / sfb_fc_d1, sfbasis.f90:719-752); a = pi/Rc
 template <typename T>
-__device__ __forceinline__ void cutoff(T d, T Rc, T& fc, T& dfc) {
+__device__ __forceinline__ void cutoff_a(T d, T Rc, T a, T& fc, T& dfc) {
   if (d >= Rc) {
     fc = T(0);
     dfc = T(0);
     return;
   }
-  const T a = T(SFB_PI) / Rc;
   T s, c;
   sincos_t(a * d, &s, &c);
   fc = T(0.5) * (c + T(1));
   dfc = T(-0.5) * a * s;
 }
+template <typename T>
+__device__ __forceinline__ void cutoff(T d, T Rc, T& fc, T& dfc) {
+  cutoff_a(d, Rc, T(SFB_PI) / Rc, fc, dfc);
+}
+
+// x / y: IEEE division in FP64; in FP32 the hardware reciprocal (~2 ulp,
+// far inside the mixed path's error budget)
+__device__ __forceinline__ double div_t(double x, double y) { return x / y; }
+__device__ __forceinline__ float div_t(float x, float y) { return __fdividef(x, y); }
 
 // radial argument x = (2 d - Rc)/Rc of chebyshev_polynomial(d, 0, Rc)
 __device__ __forceinline__ double radial_x(double d, double Rc, double) { return (2.0 * d - Rc) / Rc; }
@@ -334,6 +342,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(Po
   const int nloop = warp_max(n);
   const T r_Rc = T(ct.r_Rc), a_Rc = T(ct.a_Rc);
   const T two_over_rc = T(2) / r_Rc;
+  const T r_a = T(SFB_PI) / r_Rc, a_a = T(SFB_PI) / a_Rc;
   const int rN = GUARD ? ct.r_N : R;
   const int aN = GUARD ? ct.a_N : A;
   const bool multi = ct.multi;
@@ -363,7 +372,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(Po
     const T s = multi ? T(ct.spin[t]) : T(0);
     if (d <= r_Rc && d > T(SFB_EPS)) {
       T fc, dfc;
-      cutoff(d, r_Rc, fc, dfc);
+      cutoff_a(d, r_Rc, r_a, fc, dfc);
       const T x = radial_x(d, r_Rc, two_over_rc);
       const T x2 = x + x;
       const T sfc = s * fc;
@@ -386,9 +395,9 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(Po
     if (inA) {
       const int k = na + __popc(m & ((1u << lane) - 1u));
       if (k < b.cap_a) {
-        const T inv = T(1) / d;
+        const T inv = div_t(T(1), d);
         T fc, dfc;
-        cutoff(d, a_Rc, fc, dfc);
+        cutoff_a(d, a_Rc, a_a, fc, dfc);
         T4 u, f;
         u.x = v.x * inv;
         u.y = v.y * inv;
@@ -522,6 +531,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(Po
   const int nloop = warp_max(n);
   const T r_Rc = T(ct.r_Rc), a_Rc = T(ct.a_Rc);
   const T two_over_rc = T(2) / r_Rc;
+  const T r_a = T(SFB_PI) / r_Rc, a_a = T(SFB_PI) / a_Rc;
   const int rN = GUARD ? ct.r_N : R;
   const int aN = GUARD ? ct.a_N : A;
   const bool multi = ct.multi;
@@ -564,7 +574,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(Po
     T c = T(0);
     if (d <= r_Rc && d > T(SFB_EPS)) {
       T fc, dfc;
-      cutoff(d, r_Rc, fc, dfc);
+      cutoff_a(d, r_Rc, r_a, fc, dfc);
       const T x = radial_x(d, r_Rc, two_over_rc);
       const T x2 = x + x;
       // T_q and T_q' = q U_{q-1} (chebyshev_polynomial_d1), times dx/dd
@@ -586,7 +596,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(Po
       }
     }
     // grad_j E = c R_ij / d; the force on j is minus that
-    const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? c / d : T(0);
+    const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? div_t(c, d) : T(0);
     const T gx = inv * v.x, gy = inv * v.y, gz = inv * v.z;
     const bool inA = d <= a_Rc && d >= T(SFB_EPS);
     const unsigned m = __ballot_sync(0xffffffffu, inA) & gmask;
@@ -594,9 +604,9 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(Po
     if (inA) {
       const int k = na + __popc(m & ((1u << lane) - 1u));
       if (k < b.cap_a) {
-        const T invd = T(1) / d;
+        const T invd = div_t(T(1), d);
         T fc, dfc;
-        cutoff(d, a_Rc, fc, dfc);
+        cutoff_a(d, a_Rc, a_a, fc, dfc);
         T4 u, f;
         u.x = v.x * invd;
         u.y = v.y * invd;

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(128) k_tangent(PotDevice pd, DescBuffers b) {
     }
     const T d = v.w;
     const T s = multi ? T(ct.spin[t]) : T(0);
-    const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? T(1) / d : T(0);
+    const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? div_t(T(1), d) : T(0);
     const T p = (v.x * dlt.x + v.y * dlt.y + v.z * dlt.z) * inv;   // Rhat . delta
     dlt.w = p;
     if (d <= r_Rc && d > T(SFB_EPS)) {
