@@ -181,7 +181,8 @@ __global__ void k_scatter(int natoms, NbBuffers nb) {
 __device__ __forceinline__ int sext10i(int v) { return (v ^ 512) - 512; }
 
 // floor(a / n) for |a| < 2^20 with a reciprocal: (a + 1/2) / n is at least
-// 1/(2n) away from an integer, far more than the rounding of the product
+// 1/(2n) away from an integer, far more than the error of the product (the
+// reciprocal itself may be the ~2 ulp hardware approximation)
 __device__ __forceinline__ int floor_div_r(int a, float inv_n) {
   return (int)floorf(((float)a + 0.5f) * inv_n);
 }
@@ -242,7 +243,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
   const float rcf = g->rcf * 1.0001f + 1e-4f;
   int cnt = 0;
 
-  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const float inv_nt2 = __fdividef(1.0f, (float)nt2), inv_w1 = __fdividef(1.0f, (float)w1);
   const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
   // geometry in registers: the table stores below may alias g as far as
   // the compiler knows, which would otherwise reload these every unit
@@ -470,7 +471,7 @@ __global__ void __launch_bounds__(256) k_neighbors_cell(int ncells, NbBuffers nb
   const int cap = nb.cap;
   const int* __restrict__ cstart = nb.cell_start + g->cell_off;
   const float rcf = g->rcf * 1.0001f + 1e-4f;
-  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const float inv_nt2 = __fdividef(1.0f, (float)nt2), inv_w1 = __fdividef(1.0f, (float)w1);
 
   for (int hbase = hb; hbase < he; hbase += 32) {
     const bool home = hbase + lane < he;
@@ -745,7 +746,7 @@ __global__ void __launch_bounds__(32 * NBS_WARPS) k_neighbors_stream(int ncells,
   const int cap = nb.cap;
   const int* __restrict__ cstart = nb.cell_start + g->cell_off;
   const float rcf = g->rcf * 1.0001f + 1e-4f;
-  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const float inv_nt2 = __fdividef(1.0f, (float)nt2), inv_w1 = __fdividef(1.0f, (float)w1);
   const int ortho = g->ortho;
   const float cw0 = g->hf[0] * g->inv_nc[0], cw1 = g->hf[1] * g->inv_nc[1];
   const float zsc = g->inv_hf[2] * nc2 * 1.0001f;
@@ -937,7 +938,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbors_half(int natoms, NbBuffers
   const float sf0 = (float)nb.s_wrap[3 * i], sf1 = (float)nb.s_wrap[3 * i + 1],
               sf2 = (float)nb.s_wrap[3 * i + 2];
   const float rcf = g->rcf * 1.0001f + 1e-4f;
-  const float inv_nt2 = 1.0f / (float)nt2, inv_w1 = 1.0f / (float)w1;
+  const float inv_nt2 = __fdividef(1.0f, (float)nt2), inv_w1 = __fdividef(1.0f, (float)w1);
   const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
   const int ortho = g->ortho;
   const float hf0 = g->hf[0], hf1 = g->hf[1], ihf2 = g->inv_hf[2];
