@@ -388,6 +388,13 @@ def run_gb300(args):
     if os.path.exists(tf):
         per_atom = json.load(open(tf)).get(kernels[dom])
         traffic = None if per_atom is None else per_atom * N
+    # what limits the kernel, from the ncu capture of the same kernels
+    limiter = None
+    lf = os.path.join(ROOT, "profiles", "limiters_lisio_batch_512.txt")
+    if os.path.exists(lf):
+        lim = json.load(open(lf)).get(kernels[dom])
+        if lim:
+            limiter = dict(lim, source="profiles/ncu_full_lisio_batch_512.md (ncu --set full)")
     if dom in ("descriptor", "adjoint", "networks"):
         ach = fl[dom] * N / (dom_ms * 1e-3) / 1e12
         roof = {"bound": "fp32", "kernel": kernels[dom], "achieved": ach, "peak": peak.value,
@@ -405,6 +412,8 @@ def run_gb300(args):
                 "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                 "frac": ach / peaks.get("hbm_gbs"), "traffic": traffic,
                 "bytes_per_atom": nbytes[dom], "ms_per_launch": dom_ms}
+    if limiter:
+        roof["limiter"] = limiter
     plan32.close()
 
     # ---- plain FP64 path on the same batch
