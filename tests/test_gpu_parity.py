@@ -576,3 +576,39 @@ def test_angular_moment_form_matches_pairs(cuda, oracle, cu256, tmp_path, case):
     assert np.sqrt((dF ** 2).mean()) < 1e-4 * max(1.0, scale_F)
     dV = out["moments"]["virial"] - r64["virial"]
     assert np.abs(dV).max() < 1e-3 * max(1.0, np.abs(r64["virial"]).max())
+
+
+def test_moment_form_on_isolated_and_sparse_structures(cuda, oracle, tmp_path):
+    """Moment form where the pair sum is small or empty: isolated molecules
+    (no periodic images) and a sparse gas in which atoms have zero or one
+    angular neighbour; energies and forces against FP64 and the pair form."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    w = workloads.lisio_batch_4096(nstruc=6)
+    paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    rng = np.random.default_rng(11)
+    structs = []
+    for n in (3, 8, 20):          # molecules: compact clusters, no lattice
+        pos = rng.normal(scale=1.4, size=(n, 3))
+        structs.append((pos, rng.integers(1, 4, n).astype(np.int32), None, False))
+    for n in (12, 30):            # gas: most atoms far apart
+        pos, cell = workloads.random_cell(rng, n, density=0.004, dmin=2.5)
+        structs.append((pos, rng.integers(1, 4, n).astype(np.int32), cell, True))
+    ann = _ann(paths, w.types)
+    try:
+        r64 = ann.batch_energy_forces(structs, precision=FP64)
+        out = {}
+        for mode in ("pairs", "moments"):
+            set_option("angular_terms", mode)
+            out[mode] = ann.batch_energy_forces(structs, precision=MIXED)
+    finally:
+        set_option("angular_terms", "moments")
+        ann.release()
+    nat = np.array([len(s[1]) for s in structs])
+    for mode in ("pairs", "moments"):
+        assert np.all(np.isfinite(out[mode]["energy"])) and np.all(np.isfinite(out[mode]["forces"]))
+        dE = np.abs(out[mode]["energy"] - r64["energy"]) / nat
+        assert dE.max() < 1e-4, (mode, dE.max())
+        assert np.abs(out[mode]["forces"] - r64["forces"]).max() < 1e-3, mode
+    dE = np.abs(out["moments"]["energy"] - out["pairs"]["energy"]) / nat
+    assert dE.max() < 2e-5
