@@ -323,6 +323,12 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(Po
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
   extern __shared__ __align__(32) unsigned char smem_raw[];
+  // typespin of (central species, neighbour species): a shared table, as
+  // the per-neighbour lookups in the parameter bank would serialise
+  __shared__ float s_spin[AE_MAXT * AE_MAXT];
+  for (int q = threadIdx.x; q < pd.ntypes * AE_MAXT; q += blockDim.x)
+    s_spin[q] = pd.sp[q / AE_MAXT].cheb.spin[q % AE_MAXT];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int grp = lane / LPA, sl = lane % LPA;
@@ -369,7 +375,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(Po
       v.w = T(1e30);
     }
     const T d = v.w;
-    const T s = multi ? T(ct.spin[t]) : T(0);
+    const T s = multi ? T(s_spin[ti * AE_MAXT + t]) : T(0);
     if (d <= r_Rc && d > T(SFB_EPS)) {
       T fc, dfc;
       cutoff_a(d, r_Rc, r_a, fc, dfc);
@@ -513,6 +519,12 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(Po
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
   extern __shared__ __align__(32) unsigned char smem_raw[];
+  // typespin of (central species, neighbour species): a shared table, as
+  // the per-neighbour lookups in the parameter bank would serialise
+  __shared__ float s_spin[AE_MAXT * AE_MAXT];
+  for (int q = threadIdx.x; q < pd.ntypes * AE_MAXT; q += blockDim.x)
+    s_spin[q] = pd.sp[q / AE_MAXT].cheb.spin[q % AE_MAXT];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int grp = lane / LPA, sl = lane % LPA;
@@ -570,7 +582,7 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(Po
       v.w = T(1e30);
     }
     const T d = v.w;
-    const T s = multi ? T(ct.spin[t]) : T(0);
+    const T s = multi ? T(s_spin[ti * AE_MAXT + t]) : T(0);
     T c = T(0);
     if (d <= r_Rc && d > T(SFB_EPS)) {
       T fc, dfc;

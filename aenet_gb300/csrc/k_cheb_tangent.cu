@@ -20,6 +20,10 @@ __global__ void __launch_bounds__(128) k_tangent(PotDevice pd, DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
   extern __shared__ __align__(32) unsigned char smem_raw[];
+  __shared__ float s_spin[AE_MAXT * AE_MAXT];   // typespin by (central, neighbour) species
+  for (int q = threadIdx.x; q < pd.ntypes * AE_MAXT; q += blockDim.x)
+    s_spin[q] = pd.sp[q / AE_MAXT].cheb.spin[q % AE_MAXT];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int grp = lane / LPA, sl = lane % LPA;
@@ -71,7 +75,7 @@ __global__ void __launch_bounds__(128) k_tangent(PotDevice pd, DescBuffers b) {
       dlt.x = dlt.y = dlt.z = T(0);
     }
     const T d = v.w;
-    const T s = multi ? T(ct.spin[t]) : T(0);
+    const T s = multi ? T(s_spin[ti * AE_MAXT + t]) : T(0);
     const T inv = (d > T(SFB_EPS) && d < T(1e29)) ? div_t(T(1), d) : T(0);
     const T p = (v.x * dlt.x + v.y * dlt.y + v.z * dlt.z) * inv;   // Rhat . delta
     dlt.w = p;
