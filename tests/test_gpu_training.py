@@ -326,3 +326,27 @@ def test_fit_resumes_from_restart_file(cuda, batch, tmp_path):
     assert np.array_equal(net["W"], r3.x[:net["W"].size])
     assert abs(r33.fun - r6.fun) <= 1e-9 * abs(r6.fun)
     np.testing.assert_allclose(r33.x, r6.x, rtol=0, atol=1e-8 * np.abs(r6.x).max())
+
+
+def test_moment_tangent_matches_pair_tangent(cuda, batch):
+    """The FP32 E+F loss gradient with the angular tangent in moment form
+    (reusing the forward's moments) against the pair form: same loss and
+    gradient up to FP32 rounding."""
+    from aenet_gb300.core import MIXED, set_option
+    from aenet_gb300.train import LOSS_ENERGY_FORCES, Trainer
+    w, paths, tpaths = batch
+    E_t, F_t = _targets(w, tpaths)
+    ann = _ann(paths, w.types)
+    out = {}
+    try:
+        for mode in ("pairs", "moments"):
+            set_option("angular_terms", mode)
+            tr = Trainer(ann, _structs(w), E_t, F_t, mode=LOSS_ENERGY_FORCES, precision=MIXED)
+            out[mode] = tr.loss_and_grad()
+            tr.close()
+    finally:
+        set_option("angular_terms", "moments")
+        ann.release()
+    (l0, g0), (l1, g1) = out["pairs"], out["moments"]
+    assert abs(l1 - l0) <= 1e-5 * l0
+    assert np.linalg.norm(g1 - g0) <= 1e-4 * np.linalg.norm(g0)
