@@ -2531,12 +2531,16 @@ EXPORT int aenet_gpu_plan_descriptor_jacobian(aenet_gpu_plan* P, int atom0, int 
   if (!P || !P->pd || !P->fp64 || !d_dG_i || !d_dG_j || !d_nbl || !d_nnb) return AENET_ERR_INPUT;
   if (atom0 < 0 || count < 0 || atom0 + count > P->natoms) return AENET_ERR_INPUT;
   const PotDevice& pd = *P->pd;
-  for (int t = 0; t < pd.ntypes; ++t)
-    if (pd.sp[t].sftype != AE_SF_CHEBYSHEV) return AENET_ERR_INPUT;
+  const int sft = pd.sp[0].sftype;
+  for (int t = 1; t < pd.ntypes; ++t)
+    if (pd.sp[t].sftype != sft) return AENET_ERR_INPUT;
   DescBuffers d = desc_buffers(P, nullptr, false);
-  if (ck(ae_launch_chebyshev_jacobian(pd, d, atom0, count, pd.nsf_max, d_dG_i, d_dG_j, d_nbl,
-                                      d_nnb, (cudaStream_t)stream)))
-    return AENET_ERR_CUDA;
+  const int e = sft == AE_SF_BEHLER
+                    ? ae_launch_behler_jacobian(pd, d, atom0, count, pd.nsf_max, d_dG_i, d_dG_j,
+                                                d_nbl, d_nnb, (cudaStream_t)stream)
+                    : ae_launch_chebyshev_jacobian(pd, d, atom0, count, pd.nsf_max, d_dG_i, d_dG_j,
+                                                   d_nbl, d_nnb, (cudaStream_t)stream);
+  if (ck(e)) return AENET_ERR_CUDA;
   return AENET_OK;
 }
 

@@ -253,6 +253,9 @@ int ae_launch_chebyshev_tangent(const PotDevice& pd, const DescBuffers& b,
 int ae_launch_chebyshev_jacobian(const PotDevice& pd, const DescBuffers& b, int atom0, int count,
                                  int nsf_max, double* Ji, double* Jj, int* nbl, int* nnb,
                                  cudaStream_t s);
+int ae_launch_behler_jacobian(const PotDevice& pd, const DescBuffers& b, int atom0, int count,
+                              int nsf_max, double* Ji, double* Jj, int* nbl, int* nnb,
+                              cudaStream_t s);
 int ae_launch_behler_forward(const PotDevice& pd, const DescBuffers& b,
                              int fp64, cudaStream_t s);
 int ae_launch_behler_adjoint(const PotDevice& pd, const DescBuffers& b,

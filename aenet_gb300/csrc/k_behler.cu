@@ -519,6 +519,124 @@ int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t
   return (int)cudaGetLastError();
 }
 
+// ----------------------------------------------------------------------
+// descriptor Jacobians (FP64) for generate.x's PyTorch export: the adjoint's
+// two-sided sweep without the contraction with dE/dG -- the lane owning
+// staged neighbour j adds dG_f/dR_j of every radial function of its bucket
+// and of every angular function of every pair (j, k) to its own slot row
+// (G4/G5 carry the factor 2 of symmfunc.f90:724); the central atom's row is
+// minus the sum over the neighbours.
+// ----------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_behler_jacobian(PotDevice pd, DescBuffers b, int atom0,
+                                                         int count, int nsf_max,
+                                                         double* __restrict__ Ji,
+                                                         double* __restrict__ Jj,
+                                                         int* __restrict__ nbl,
+                                                         int* __restrict__ nnb) {
+  using T = double;
+  using T4 = double4_32a;
+  extern __shared__ __align__(32) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int r = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (r >= count) return;
+  const int i = atom0 + r;
+  unsigned char* base = smem_raw + behler_smem_per_warp<T>(b.cap, pd.nsf_pad, false) * warp;
+  T4* sR = reinterpret_cast<T4*>(base);
+  int* sslot = reinterpret_cast<int*>(sR + b.cap);
+  const int ti = b.types[i];
+  const BehlerTable* tab = table_of<T>(pd, ti);
+  const int nt = pd.ntypes;
+  const int n = b.nb_cnt[i];
+  const T4* __restrict__ vec = reinterpret_cast<const T4*>(b.nb_vec) + (size_t)i * b.cap;
+  const int* __restrict__ jt = b.nb_jt + (size_t)i * b.cap;
+  const size_t rs = (size_t)nsf_max * 3;
+  double* __restrict__ Jrow = Jj + (size_t)r * b.cap * rs;
+  if (lane == 0) nnb[r] = n;
+  for (int a = lane; a < n; a += 32) {
+    for (size_t q = 0; q < rs; ++q) Jrow[(size_t)a * rs + q] = 0.0;
+    nbl[(size_t)r * b.cap + a] = jt[a] & AE_INDEX_MASK;
+  }
+  int bstart[AE_MAXT + 1];
+  const int nst = stage_buckets<T>(vec, jt, n, nt, T(tab->rc_max), sR, sslot, bstart, lane);
+  __syncwarp();
+  for (int j = lane; j < nst; j += 32) {
+    int tj = 0;
+    for (int s2 = 0; s2 < nt; ++s2)
+      if (j >= bstart[s2 + 1]) tj = s2 + 1;
+    if (tj >= nt) tj = nt - 1;
+    const T4 Rj = sR[j];
+    const T invj = T(1) / Rj.w;
+    const T ux = Rj.x * invj, uy = Rj.y * invj, uz = Rj.z * invj;
+    double* Ja = Jrow + (size_t)sslot[j] * rs;
+    // radial functions of bucket tj
+    for (int q = tab->rad_off[tj]; q < tab->rad_off[tj + 1]; ++q) {
+      const Fn<T> f = load_fn<T>(&tab->fn[q]);
+      T v, dv;
+      radial_fn(f, Rj.w, v, dv);
+      Ja[f.out * 3] += dv * ux;
+      Ja[f.out * 3 + 1] += dv * uy;
+      Ja[f.out * 3 + 2] += dv * uz;
+    }
+    // angular functions of every pair (j, k)
+    for (int k = 0; k < nst; ++k) {
+      if (k == j) continue;
+      int tk = 0;
+      for (int s2 = 0; s2 < nt; ++s2)
+        if (k >= bstart[s2 + 1]) tk = s2 + 1;
+      const int lo = min(tj, tk), hi = max(tj, tk);
+      const int f0 = tab->ang_off[lo * nt + hi], f1e = tab->ang_off[lo * nt + hi + 1];
+      if (f0 == f1e) continue;
+      const T4 Rk = sR[k];
+      const T dxx = Rk.x - Rj.x, dyy = Rk.y - Rj.y, dzz = Rk.z - Rj.z;
+      const T rjk2 = dxx * dxx + dyy * dyy + dzz * dzz;
+      const T rjk = sqrt(rjk2);
+      const T invk = T(1) / Rk.w;
+      const T vx = Rk.x * invk, vy = Rk.y * invk, vz = Rk.z * invk;
+      T cosv = ux * vx + uy * vy + uz * vz;
+      cosv = fmax(T(-1), fmin(T(1), cosv));
+      const T rij2 = Rj.w * Rj.w, rik2 = Rk.w * Rk.w;
+      const T ijk = rjk > T(1e-8) ? T(1) / rjk : T(0);
+      T rc_cur = T(-1), fij = 0, dfij = 0, fik = 0, dfik = 0, fjk = 0, dfjk = 0;
+      for (int q = f0; q < f1e; ++q) {
+        const Fn<T> f = load_fn<T>(&tab->fn[q]);
+        if (f.Rc != rc_cur) {
+          rc_cur = f.Rc;
+          cutfn(Rj.w, rc_cur, fij, dfij);
+          cutfn(Rk.w, rc_cur, fik, dfik);
+          cutfn(rjk, rc_cur, fjk, dfjk);
+        }
+        T F1v, dF1v;
+        f1(f, cosv, F1v, dF1v);
+        T Sc, Sij, Sjk = T(0);
+        if (f.kind == 4) {
+          const T E = T(2) * exp_t(-f.p3 * (rij2 + rik2 + rjk2));
+          Sc = E * dF1v * fij * fik * fjk;
+          Sij = E * F1v * fik * fjk * (dfij - T(2) * f.p3 * Rj.w * fij);
+          Sjk = E * F1v * fij * fik * (dfjk - T(2) * f.p3 * rjk * fjk);
+        } else {
+          const T E = T(2) * exp_t(-f.p3 * (rij2 + rik2));
+          Sc = E * dF1v * fij * fik;
+          Sij = E * F1v * fik * (dfij - T(2) * f.p3 * Rj.w * fij);
+        }
+        // grad_j = Sc (Rhat_k - cos Rhat_j)/r_ij + Sij Rhat_j - Sjk Rhat_jk
+        const T cj = Sc * invj;
+        Ja[f.out * 3] += cj * (vx - cosv * ux) + Sij * ux - Sjk * ijk * dxx;
+        Ja[f.out * 3 + 1] += cj * (vy - cosv * uy) + Sij * uy - Sjk * ijk * dyy;
+        Ja[f.out * 3 + 2] += cj * (vz - cosv * uz) + Sij * uz - Sjk * ijk * dzz;
+      }
+    }
+  }
+  __syncwarp();
+  const int nq = pd.sp[ti].nsf * 3;
+  for (int q = lane; q < (int)rs; q += 32) {
+    double acc = 0.0;
+    if (q < nq)
+      for (int a = 0; a < n; ++a) acc -= Jrow[(size_t)a * rs + q];
+    Ji[(size_t)r * rs + q] = acc;
+  }
+}
+
 }  // namespace
 
 int ae_launch_behler_forward(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStream_t s) {
@@ -529,4 +647,18 @@ int ae_launch_behler_forward(const PotDevice& pd, const DescBuffers& b, int fp64
 int ae_launch_behler_adjoint(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStream_t s) {
   if (b.natoms <= 0) return 0;
   return fp64 ? launch<double>(pd, b, true, s) : launch<float>(pd, b, true, s);
+}
+
+int ae_launch_behler_jacobian(const PotDevice& pd, const DescBuffers& b, int atom0, int count,
+                              int nsf_max, double* Ji, double* Jj, int* nbl, int* nnb,
+                              cudaStream_t s) {
+  if (count <= 0) return 0;
+  const int warps = 4;
+  const size_t smem = behler_smem_per_warp<double>(b.cap, pd.nsf_pad, false) * warps;
+  if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_behler_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_behler_jacobian<<<(count + warps - 1) / warps, warps * 32, smem, s>>>(pd, b, atom0, count,
+                                                                         nsf_max, Ji, Jj, nbl, nnb);
+  return (int)cudaGetLastError();
 }

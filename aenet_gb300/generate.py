@@ -12,8 +12,7 @@ The descriptors come from the GPU FP64 path: the potentials are loaded with
 identity normalisation, so the plan's descriptor rows are the raw values.
 With ``forces_percent`` the descriptor Jacobians of that share of the
 structures are written beside the training set in the PyTorch export
-format of generate.x's FORCES keyword (aenet_gb300/pytorch_export.py,
-Chebyshev bases).
+format of generate.x's FORCES keyword (aenet_gb300/pytorch_export.py).
 """
 import os
 import tempfile

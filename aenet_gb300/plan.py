@@ -220,7 +220,7 @@ class Plan:
 
     def jacobian(self, atom0=0, count=None, nsf_max=None):
         """Raw FP64 descriptor Jacobians of atoms [atom0, atom0 + count) from
-        the neighbour table of the last run (Chebyshev bases, FP64 plans):
+        the neighbour table of the last run (FP64 plans, Chebyshev or Behler):
         (dG/dR_i [count, nsf_max, 3], dG/dR_j [count, cap, nsf_max, 3],
         neighbour atom indices [count, cap], neighbour counts [count]) as
         CUDA tensors (aenet_gpu_plan_descriptor_jacobian)."""

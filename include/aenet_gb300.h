@@ -205,8 +205,8 @@ int aenet_gpu_plan_load_descriptors(aenet_gpu_plan* plan, const double* G, int l
  * d_dG_j[count][cap][nsf_max][3]; d_nbl[count][cap] the neighbours' 0-based
  * atom indices in the batch (periodic images repeat an index), d_nnb[count]
  * the neighbour counts.  Reads the neighbour table of the plan's last run
- * (aenet_gpu_plan_run or _forward), so call it after one; FP64 plans and
- * Chebyshev bases only (AENET_ERR_INPUT otherwise).  nsf_max is
+ * (aenet_gpu_plan_run or _forward), so call it after one; FP64 plans only
+ * (AENET_ERR_INPUT otherwise), Chebyshev or Behler bases.  nsf_max is
  * aenet_nsf_max, cap the value of aenet_gpu_plan_neighbour_capacity. */
 int aenet_gpu_plan_neighbour_capacity(const aenet_gpu_plan* plan);
 int aenet_gpu_plan_descriptor_jacobian(aenet_gpu_plan* plan, int atom0, int count,

@@ -612,3 +612,43 @@ def test_moment_form_on_isolated_and_sparse_structures(cuda, oracle, tmp_path):
         assert np.abs(out[mode]["forces"] - r64["forces"]).max() < 1e-3, mode
     dE = np.abs(out["moments"]["energy"] - out["pairs"]["energy"]) / nat
     assert dE.max() < 2e-5
+
+
+def test_behler_descriptor_jacobians_match_oracle(cuda, oracle, rutile):
+    """PyTorch-export Jacobians for Behler bases (G1-G5): every neighbour
+    slot's and the central atom's FP64 derivatives against the oracle's
+    symmfunc restatement (stp_eval with derivatives), matched by pair
+    vector."""
+    import torch
+    from aenet_gb300.core import FP64
+    from aenet_gb300.plan import Plan
+    w, paths = rutile
+    s = w.structures[0]
+    oracle.load(w.types, paths)
+    ann = _ann(paths, w.types)
+    try:
+        plan = Plan([s.natoms], s.cell[None], np.array([1], dtype=np.int32), precision=FP64)
+        plan.run(torch.tensor(s.positions, device="cuda"),
+                 torch.tensor(s.types.astype(np.int32), device="cuda"), forces=False)
+        plan.check()
+        Ji, Jj, nbl, nnb = (x.cpu().numpy() for x in plan.jacobian())
+        vec = plan.neighbors()[3].cpu().numpy()
+        plan.close()
+    finally:
+        ann.release()
+    _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types)
+    for a in range(0, s.natoms, 7):
+        nbcoo, _, nblist, nbt = nb[a]
+        G, di, dj = oracle.descriptor(centres[a], int(s.types[a]), nbcoo, nbt, scaled=False,
+                                      deriv=True)
+        nsf = G.size
+        m = int(nnb[a])
+        assert m == len(nblist)
+        scale = max(1.0, np.abs(dj).max())
+        np.testing.assert_allclose(Ji[a, :nsf], di, rtol=0, atol=1e-9 * scale)
+        R_ref = nbcoo - centres[a]
+        for q in range(m):
+            k = int(np.argmin(np.abs(R_ref - vec[a, q, :3]).sum(1)))
+            assert np.abs(R_ref[k] - vec[a, q, :3]).max() < 1e-9
+            assert nbl[a, q] + 1 == nblist[k]
+            np.testing.assert_allclose(Jj[a, q, :nsf], dj[k], rtol=0, atol=1e-9 * scale)
