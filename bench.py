@@ -530,9 +530,9 @@ def run_gb300(args):
     else:
         ann.release()
 
-    launches_per_step = 15   # types, 6 neighbour-search kernels, descriptor, 3 species-
-    #                          partition kernels, tensor-core networks, energy reduction,
-    #                          adjoint, force output
+    launches_per_step = 16   # types, 6 neighbour-search kernels, descriptor, 3 species-
+    #                          partition kernels, tensor-core networks, 2 energy-reduction
+    #                          kernels, adjoint, force output
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
