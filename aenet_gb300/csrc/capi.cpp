@@ -883,9 +883,11 @@ struct HostPlanCache {
   char* io = nullptr;
   size_t io_bytes = 0;
   cudaStream_t stream = nullptr;
+  unsigned* status_h = nullptr;   // pinned: the status read back stays asynchronous
   ~HostPlanCache() {
     if (io) cudaFree(io);
     if (stream) cudaStreamDestroy(stream);
+    if (status_h) cudaFreeHost(status_h);
   }
   void reset() {
     plan.reset();
@@ -894,7 +896,15 @@ struct HostPlanCache {
     io_bytes = 0;
   }
 };
-HostPlanCache g_cache;
+// Large host-buffer batches run as up to AE_HOST_CHUNKS chunks of whole
+// structures, each with its own cached plan and stream, so that one
+// chunk's copies overlap the others' kernels.
+constexpr int AE_HOST_CHUNKS = 4;
+constexpr long long AE_CHUNK_ATOMS = 131072;   // atoms per chunk at least
+HostPlanCache g_cache[AE_HOST_CHUNKS];
+void host_cache_reset() {
+  for (auto& c : g_cache) c.reset();
+}
 void nlist_release();   // drops the neighbour-list entry point's workspace
 }  // namespace
 
@@ -1335,7 +1345,7 @@ EXPORT void aenet_final(int* stat) {
   std::lock_guard<std::mutex> lk(g_mu);
   *stat = AENET_OK;
   if (g.init) {
-    g_cache.reset();
+    host_cache_reset();
     nlist_release();
     g.blob.reset();
     g.pots.clear();
@@ -2745,9 +2755,8 @@ int ae_periodic_geom(StructGeom* G, const double* lattice, int natoms, double rc
 namespace {
 
 
-bool cache_matches(int nstruc, const int* natoms, const double* lattices, const int* pbc,
-                   int precision) {
-  HostPlanCache& c = g_cache;
+bool cache_matches(const HostPlanCache& c, int nstruc, const int* natoms, const double* lattices,
+                   const int* pbc, int precision) {
   if (!c.plan || c.precision != precision || (int)c.natoms.size() != nstruc || c.isolated) return false;
   if (memcmp(c.natoms.data(), natoms, 4 * (size_t)nstruc)) return false;
   for (int s = 0; s < nstruc; ++s)
@@ -2756,83 +2765,176 @@ bool cache_matches(int nstruc, const int* natoms, const double* lattices, const 
   return true;
 }
 
+// One chunk: (re)build its plan when the layout changed or cap > 0 asks
+// for a larger capacity, then enqueue on its stream the copies in, the run
+// and the status read back.  Nothing waits here.
+int chunk_submit(HostPlanCache& c, int nstruc, const int* natoms, const double* coords,
+                 const int* type_ids, const double* lattices, const int* pbc, int precision,
+                 bool want_E_atoms, bool want_virial, bool want_forces, int cap) {
+  int st = 0;
+  if (cap > 0 || !cache_matches(c, nstruc, natoms, lattices, pbc, precision)) {
+    c.reset();
+    c.plan.reset(plan_new(nstruc, natoms, lattices, pbc, coords, precision, &g.pd, aenet_Rc_max,
+                          cap, false, &st));
+    if (!c.plan) return st ? st : AENET_ERR_CUDA;
+    c.natoms.assign(natoms, natoms + nstruc);
+    c.pbc.assign(nstruc, 1);
+    c.isolated = false;
+    for (int q = 0; q < nstruc; ++q) {
+      c.pbc[q] = pbc ? (pbc[q] ? 1 : 0) : 1;
+      if (!c.pbc[q]) c.isolated = true;   // binning box follows the coordinates
+    }
+    c.lattices.assign(lattices ? lattices : nullptr, lattices ? lattices + 9 * (size_t)nstruc : nullptr);
+    c.precision = precision;
+  }
+  if (!c.stream && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+    return AENET_ERR_CUDA;
+  if (!c.status_h && cudaHostAlloc(&c.status_h, 16, cudaHostAllocDefault) != cudaSuccess) {
+    c.status_h = nullptr;
+    return AENET_ERR_CUDA;
+  }
+  aenet_gpu_plan* P = c.plan.get();
+  const int N = P->natoms;
+  const size_t bytes = 24 * (size_t)N + 4 * (size_t)N + 8 * (size_t)nstruc + 8 * (size_t)N +
+                       24 * (size_t)N + 72 * (size_t)nstruc + 1024;
+  if (c.io_bytes < bytes) {
+    if (c.io) cudaFree(c.io);
+    c.io = nullptr;
+    if (cudaMalloc(&c.io, bytes) != cudaSuccess) return AENET_ERR_CUDA;
+    c.io_bytes = bytes;
+  }
+  double* d_c = (double*)c.io;
+  double* d_F = d_c + 3 * (size_t)N;
+  double* d_Ea = d_F + 3 * (size_t)N;
+  double* d_E = d_Ea + N;
+  double* d_V = d_E + nstruc;
+  int* d_t = (int*)(d_V + 9 * (size_t)nstruc);
+  cudaStream_t s = c.stream;
+  *c.status_h = 0;
+  if (cudaMemsetAsync(P->status, 0, 4, s) ||
+      cudaMemcpyAsync(d_c, coords, 24 * (size_t)N, cudaMemcpyHostToDevice, s) ||
+      cudaMemcpyAsync(d_t, type_ids, 4 * (size_t)N, cudaMemcpyHostToDevice, s))
+    return AENET_ERR_CUDA;
+  const unsigned flags =
+      (want_forces ? AENET_GPU_FORCES : 0u) | (want_virial ? AENET_GPU_VIRIAL : 0u);
+  st = aenet_gpu_plan_run(P, d_c, d_t, d_E, want_E_atoms ? d_Ea : nullptr,
+                          (want_forces || want_virial) ? d_F : nullptr,
+                          want_virial ? d_V : nullptr, flags, s);
+  if (st) return st;
+  return cudaMemcpyAsync(c.status_h, P->status, 4, cudaMemcpyDeviceToHost, s) ? AENET_ERR_CUDA : 0;
+}
+
+// The chunk's results back to the caller's arrays (enqueued after every
+// chunk's run, so that a pageable destination, which makes the copy wait
+// for its data, holds up no other chunk's kernels).
+int chunk_collect(HostPlanCache& c, int nstruc, double* E, double* E_atoms, double* F,
+                  double* virial, bool want_forces) {
+  aenet_gpu_plan* P = c.plan.get();
+  const int N = P->natoms;
+  double* d_c = (double*)c.io;
+  double* d_F = d_c + 3 * (size_t)N;
+  double* d_Ea = d_F + 3 * (size_t)N;
+  double* d_E = d_Ea + N;
+  double* d_V = d_E + nstruc;
+  cudaStream_t s = c.stream;
+  if (E && cudaMemcpyAsync(E, d_E, 8 * (size_t)nstruc, cudaMemcpyDeviceToHost, s))
+    return AENET_ERR_CUDA;
+  if (E_atoms && cudaMemcpyAsync(E_atoms, d_Ea, 8 * (size_t)N, cudaMemcpyDeviceToHost, s))
+    return AENET_ERR_CUDA;
+  if (F && want_forces && cudaMemcpyAsync(F, d_F, 24 * (size_t)N, cudaMemcpyDeviceToHost, s))
+    return AENET_ERR_CUDA;
+  if (virial && cudaMemcpyAsync(virial, d_V, 72 * (size_t)nstruc, cudaMemcpyDeviceToHost, s))
+    return AENET_ERR_CUDA;
+  return 0;
+}
+
+// after a failure: let every chunk's queued work finish, then drop the plans
+int drain_and_reset(int st) {
+  for (auto& c : g_cache)
+    if (c.stream) cudaStreamSynchronize(c.stream);
+  host_cache_reset();
+  return st;
+}
+
 int batch_host(int nstruc, const int* natoms, const double* coords, const int* type_ids,
                const double* lattices, const int* pbc, int precision, double* E,
                double* E_atoms, double* F, double* virial, bool want_forces) {
   int st = ensure_device();
   if (st) return st;
-  int cap = 0;
-  for (int attempt = 0; attempt < 4; ++attempt) {
-    HostPlanCache& c = g_cache;
-    if (!(attempt == 0 && cache_matches(nstruc, natoms, lattices, pbc, precision))) {
-      c.reset();
-      c.plan.reset(plan_new(nstruc, natoms, lattices, pbc, coords, precision, &g.pd, aenet_Rc_max,
-                            cap, false, &st));
-      if (!c.plan) return st;
-      c.natoms.assign(natoms, natoms + nstruc);
-      c.pbc.assign(nstruc, 1);
-      c.isolated = false;
-      for (int q = 0; q < nstruc; ++q) {
-        c.pbc[q] = pbc ? (pbc[q] ? 1 : 0) : 1;
-        if (!c.pbc[q]) c.isolated = true;   // binning box follows the coordinates
+  // chunks of whole structures with about equal atom counts
+  long long Ntot = 0;
+  for (int q = 0; q < nstruc; ++q) Ntot += natoms[q];
+  int C = (int)std::min<long long>(AE_HOST_CHUNKS, std::max<long long>(1, Ntot / AE_CHUNK_ATOMS));
+  C = std::min(C, nstruc);
+  int sb[AE_HOST_CHUNKS + 1];
+  long long ab[AE_HOST_CHUNKS + 1];
+  sb[0] = 0;
+  ab[0] = 0;
+  {
+    long long acc = 0;
+    int k = 1;
+    for (int q = 0; q < nstruc && k < C; ++q) {
+      acc += natoms[q];
+      if (acc * C >= Ntot * k) {
+        sb[k] = q + 1;
+        ab[k] = acc;
+        ++k;
       }
-      c.lattices.assign(lattices ? lattices : nullptr, lattices ? lattices + 9 * (size_t)nstruc : nullptr);
-      c.precision = precision;
-      if (!c.stream && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
-        return AENET_ERR_CUDA;
     }
-    aenet_gpu_plan* P = c.plan.get();
-    const int N = P->natoms;
-    double *d_c = nullptr, *d_E = nullptr, *d_Ea = nullptr, *d_F = nullptr, *d_V = nullptr;
-    int* d_t = nullptr;
-    size_t bytes = 24 * (size_t)N + 4 * (size_t)N + 8 * (size_t)nstruc + 8 * (size_t)N +
-                   24 * (size_t)N + 72 * (size_t)nstruc + 1024;
-    if (c.io_bytes < bytes) {
-      if (c.io) cudaFree(c.io);
-      c.io = nullptr;
-      if (cudaMalloc(&c.io, bytes) != cudaSuccess) return AENET_ERR_CUDA;
-      c.io_bytes = bytes;
+    for (; k < C; ++k) {   // fewer structures than cut points: empty chunks are dropped below
+      sb[k] = nstruc;
+      ab[k] = Ntot;
     }
-    char* mem = c.io;
-    d_c = (double*)mem;
-    d_F = d_c + 3 * (size_t)N;
-    d_Ea = d_F + 3 * (size_t)N;
-    d_E = d_Ea + N;
-    d_V = d_E + nstruc;
-    d_t = (int*)(d_V + 9 * (size_t)nstruc);
-    cudaStream_t s = c.stream;
-    cudaMemsetAsync(P->status, 0, 4, s);
-    cudaMemcpyAsync(d_c, coords, 24 * (size_t)N, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_t, type_ids, 4 * (size_t)N, cudaMemcpyHostToDevice, s);
-    unsigned flags = (want_forces ? AENET_GPU_FORCES : 0u) | (virial ? AENET_GPU_VIRIAL : 0u);
-    st = aenet_gpu_plan_run(P, d_c, d_t, d_E, E_atoms ? d_Ea : nullptr,
-                            (want_forces || virial) ? d_F : nullptr, virial ? d_V : nullptr, flags, s);
-    unsigned status = 0;
-    if (!st) {
-      cudaMemcpyAsync(&status, P->status, 4, cudaMemcpyDeviceToHost, s);
-      if (E) cudaMemcpyAsync(E, d_E, 8 * (size_t)nstruc, cudaMemcpyDeviceToHost, s);
-      if (E_atoms) cudaMemcpyAsync(E_atoms, d_Ea, 8 * (size_t)N, cudaMemcpyDeviceToHost, s);
-      if (F && want_forces) cudaMemcpyAsync(F, d_F, 24 * (size_t)N, cudaMemcpyDeviceToHost, s);
-      if (virial) cudaMemcpyAsync(virial, d_V, 72 * (size_t)nstruc, cudaMemcpyDeviceToHost, s);
-      if (cudaStreamSynchronize(s) != cudaSuccess) st = AENET_ERR_CUDA;
+    sb[C] = nstruc;
+    ab[C] = Ntot;
+  }
+  int caps[AE_HOST_CHUNKS] = {0, 0, 0, 0};
+  bool pending[AE_HOST_CHUNKS];
+  for (int k = 0; k < C; ++k) pending[k] = sb[k + 1] > sb[k];
+  for (int k = C; k < AE_HOST_CHUNKS; ++k) g_cache[k].reset();   // the layout changed
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    for (int k = 0; k < C; ++k) {
+      if (!pending[k]) continue;
+      const int s0 = sb[k], ns = sb[k + 1] - s0;
+      const size_t a0 = (size_t)ab[k];
+      st = chunk_submit(g_cache[k], ns, natoms + s0, coords + 3 * a0, type_ids + a0,
+                        lattices ? lattices + 9 * (size_t)s0 : nullptr, pbc ? pbc + s0 : nullptr,
+                        precision, E_atoms != nullptr, virial != nullptr, want_forces, caps[k]);
+      if (st) return drain_and_reset(st);
     }
-    if (st) {
-      c.reset();
-      return st;
+    for (int k = 0; k < C; ++k) {
+      if (!pending[k]) continue;
+      const int s0 = sb[k], ns = sb[k + 1] - s0;
+      const size_t a0 = (size_t)ab[k];
+      st = chunk_collect(g_cache[k], ns, E ? E + s0 : nullptr, E_atoms ? E_atoms + a0 : nullptr,
+                         F ? F + 3 * a0 : nullptr, virial ? virial + 9 * (size_t)s0 : nullptr,
+                         want_forces);
+      if (st) return drain_and_reset(st);
     }
-    if (status & (AE_ST_BAD_COORD)) return AENET_ERR_INPUT;
-    if (status & AE_ST_BAD_TYPE) return AENET_ERR_TYPE;
-    if (status & AE_ST_TC_TIMEOUT) {
-      c.reset();
-      return AENET_ERR_CUDA;
+    bool again = false;
+    int err = 0;
+    for (int k = 0; k < C; ++k) {
+      if (!pending[k]) continue;
+      HostPlanCache& c = g_cache[k];
+      if (cudaStreamSynchronize(c.stream) != cudaSuccess) return drain_and_reset(AENET_ERR_CUDA);
+      const unsigned status = *c.status_h;
+      pending[k] = false;
+      if (status & AE_ST_TC_TIMEOUT) {
+        c.reset();
+        err = AENET_ERR_CUDA;
+      } else if (status & AE_ST_BAD_COORD) {
+        err = err ? err : AENET_ERR_INPUT;
+      } else if (status & AE_ST_BAD_TYPE) {
+        err = err ? err : AENET_ERR_TYPE;
+      } else if (status & (AE_ST_NB_OVERFLOW | AE_ST_CELL_OVERFLOW)) {
+        // retry with larger capacities (the angular capacity follows cap)
+        caps[k] = c.plan->cap * 2;
+        pending[k] = true;
+        again = true;
+      }
     }
-    if (status & (AE_ST_NB_OVERFLOW | AE_ST_CELL_OVERFLOW)) {
-      // retry with larger capacities (the angular capacity follows cap)
-      cap = P->cap * 2;
-      c.reset();
-      continue;
-    }
-    return 0;
+    if (err) return err;
+    if (!again) return 0;
   }
   return AENET_ERR_MALLOC;
 }

@@ -28,6 +28,9 @@
 #define AE_MAXG4 64          // Behler angular functions per triple type
 #define AE_MAXG2 64          // Behler radial functions per pair type
 #define AE_MOMA 7            // angular functions (order + 1) of the moment form
+// static shared memory a kernel may add to its dynamic allocation; the
+// launchers opt in to large dynamic shared memory once the sum passes 48 KB
+#define AE_STATIC_SMEM 1024
 
 // status bits written by kernels into a device word
 #define AE_ST_NB_OVERFLOW 1u

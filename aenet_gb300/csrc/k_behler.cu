@@ -508,11 +508,11 @@ int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t
   if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
   const int blocks = (b.natoms + warps - 1) / warps;
   if (adjoint) {
-    if (smem > 48 * 1024)
+    if (smem + AE_STATIC_SMEM > 48 * 1024)
       cudaFuncSetAttribute(k_behler_adjoint<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_behler_adjoint<T><<<blocks, warps * 32, smem, s>>>(pd, b);
   } else {
-    if (smem > 48 * 1024)
+    if (smem + AE_STATIC_SMEM > 48 * 1024)
       cudaFuncSetAttribute(k_behler_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_behler_forward<T><<<blocks, warps * 32, smem, s>>>(pd, b);
   }
@@ -656,7 +656,7 @@ int ae_launch_behler_jacobian(const PotDevice& pd, const DescBuffers& b, int ato
   const int warps = 4;
   const size_t smem = behler_smem_per_warp<double>(b.cap, pd.nsf_pad, false) * warps;
   if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
-  if (smem > 48 * 1024)
+  if (smem + AE_STATIC_SMEM > 48 * 1024)
     cudaFuncSetAttribute(k_behler_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_behler_jacobian<<<(count + warps - 1) / warps, warps * 32, smem, s>>>(pd, b, atom0, count,
                                                                          nsf_max, Ji, Jj, nbl, nnb);

@@ -858,12 +858,12 @@ int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t
   const int blocks = (b.natoms + atoms_per_block - 1) / atoms_per_block;
   if (adjoint) {
     auto kern = k_adjoint<T, R, A, LPA, GUARD, MOM>;
-    if (smem > 48 * 1024)
+    if (smem + AE_STATIC_SMEM > 48 * 1024)
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<blocks, warps * 32, smem, s>>>(pd, b);
   } else {
     auto kern = k_forward<T, R, A, LPA, GUARD, MOM>;
-    if (smem > 48 * 1024)
+    if (smem + AE_STATIC_SMEM > 48 * 1024)
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<blocks, warps * 32, smem, s>>>(pd, b);
   }

@@ -457,7 +457,7 @@ int launch_tangent_mom(const PotDevice& pd, const DescBuffers& b, cudaStream_t s
   if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
   const int blocks = (b.natoms + groups - 1) / groups;
   auto kern = k_tangent_mom<R, A, LPA>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem + AE_STATIC_SMEM > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kern<<<blocks, warps * 32, smem, s>>>(pd, b);
   return (int)cudaGetLastError();
 }
@@ -473,7 +473,7 @@ int launch_tangent(const PotDevice& pd, const DescBuffers& b, cudaStream_t s) {
   if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
   const int blocks = (b.natoms + groups - 1) / groups;
   auto kern = k_tangent<T, R, A, LPA>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem + AE_STATIC_SMEM > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kern<<<blocks, warps * 32, smem, s>>>(pd, b);
   return (int)cudaGetLastError();
 }

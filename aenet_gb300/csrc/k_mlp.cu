@@ -309,11 +309,11 @@ int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStrea
   int maxb = nsm * 4;
   if (blocks > maxb) blocks = maxb;
   if (fp64) {
-    if (smem > 48 * 1024)
+    if (smem + AE_STATIC_SMEM > 48 * 1024)
       cudaFuncSetAttribute(k_mlp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_mlp<double><<<blocks, warps * 32, smem, s>>>(pd, b, pd.w64, wtotal);
   } else {
-    if (smem > 48 * 1024)
+    if (smem + AE_STATIC_SMEM > 48 * 1024)
       cudaFuncSetAttribute(k_mlp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_mlp<float><<<blocks, warps * 32, smem, s>>>(pd, b, pd.w32, wtotal);
   }

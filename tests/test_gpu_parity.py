@@ -652,3 +652,32 @@ def test_behler_descriptor_jacobians_match_oracle(cuda, oracle, rutile):
             assert np.abs(R_ref[k] - vec[a, q, :3]).max() < 1e-9
             assert nbl[a, q] + 1 == nblist[k]
             np.testing.assert_allclose(Jj[a, q, :nsf], dj[k], rtol=0, atol=1e-9 * scale)
+
+
+def test_host_batch_runs_in_chunks_like_one_plan(cuda, oracle, tmp_path):
+    """Large host-buffer batches run as chunks of whole structures on
+    separate streams: 16 cells repeated to ~300k atoms give, copy for copy,
+    the energies, forces and virials of the 16 cells evaluated alone (FP64:
+    identical to rounding of the force sums; mixed: same kernels, FP32
+    noise only)."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED
+    w = workloads.lisio_batch_4096(nstruc=16)
+    paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    base = [(s.positions, s.types, s.cell, True) for s in w.structures]
+    nat = np.array([len(s[1]) for s in base])
+    reps = int(np.ceil(300000 / nat.sum()))
+    big = base * reps
+    ann = _ann(paths, w.types)
+    try:
+        for prec, tol in ((FP64, 1e-11), (MIXED, 1e-5)):
+            one = ann.batch_energy_forces(base, precision=prec, virial=True)
+            many = ann.batch_energy_forces(big, precision=prec, virial=True)
+            E = many["energy"].reshape(reps, len(base))
+            assert np.abs(E - one["energy"][None]).max() / nat.min() < tol
+            F = many["forces"].reshape(reps, nat.sum(), 3)
+            assert np.abs(F - one["forces"][None]).max() < 100 * tol
+            V = many["virial"].reshape(reps, len(base), 3, 3)
+            assert np.abs(V - one["virial"][None]).max() < 1e3 * tol * max(1, np.abs(one["virial"]).max())
+    finally:
+        ann.release()
