@@ -2048,7 +2048,7 @@ int plan_train_alloc(aenet_gpu_plan* P) {
   size_t o_ce = take(8 * (size_t)P->nstruc);
   size_t o_ls = take(8 * (size_t)P->nstruc);
   size_t o_u = take(4 * tsz * N);
-  size_t o_p = take(8 * (size_t)pd.ntypes * ae_wgrad_nblk() * ae_wgrad_wcap(pd));
+  size_t o_p = take(8 * (size_t)pd.ntypes * ae_wgrad_nblk(pd.ntypes) * ae_wgrad_wcap(pd));
   if (cudaMalloc(&P->tmem, off) != cudaSuccess) {
     P->tmem = nullptr;
     return AENET_ERR_CUDA;

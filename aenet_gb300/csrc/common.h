@@ -292,7 +292,7 @@ int ae_launch_loss(int nstruc, const StructGeom* geom, const double* E_struct, c
                    double E_scale, double* cE, void* U, double* loss_s, double* loss, int fp64,
                    cudaStream_t s);
 int ae_wgrad_wcap(const PotDevice& pd);
-int ae_wgrad_nblk();
+int ae_wgrad_nblk(int ntypes);
 int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_off, const void* G,
                         const void* V, const int* atom_struct, const double* cE, double cF,
                         int physical, double* partial, double* grad, int fp64, cudaStream_t s);

@@ -522,12 +522,19 @@ int ae_wgrad_wcap(const PotDevice& pd) {
   return (w + 31) & ~31;
 }
 
-int ae_wgrad_nblk() { return 96; }
+// blocks per species: about three resident blocks (the shared-memory limit
+// of the kernel) on every SM over all species, at least 96
+int ae_wgrad_nblk(int ntypes) {
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return max(96, (3 * nsm + ntypes - 1) / max(1, ntypes));
+}
 
 int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_off, const void* G,
                         const void* V, const int* atom_struct, const double* cE, double cF,
                         int physical, double* partial, double* grad, int fp64, cudaStream_t s) {
-  const int warps = 8, nblk = ae_wgrad_nblk();
+  const int warps = 8, nblk = ae_wgrad_nblk(pd.ntypes);
   const bool tang = V != nullptr;
   WgradArgs A{};
   A.ntypes = pd.ntypes;
