@@ -193,11 +193,6 @@ __device__ __forceinline__ float pair_length(float dd2) {
   return dd2 > 0.f ? dd2 * rsqrtf(dd2) : 0.f;
 }
 
-__device__ __forceinline__ int floor_div(int a, int n) {
-  int q = a / n;
-  return (a % n != 0 && (a < 0)) ? q - 1 : q;
-}
-
 template <typename T4>
 struct VecOut;
 template <>
