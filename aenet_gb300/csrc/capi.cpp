@@ -277,6 +277,8 @@ struct State {
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
+  int gen = 0;                // bumped by every option change and table build: captured
+                              // graphs of the host-buffer path are redone after it
   PotDevice pd{};
   std::unique_ptr<DevBlob> blob;
   std::vector<std::vector<unsigned char>> behler_host;
@@ -489,6 +491,7 @@ std::vector<unsigned char> make_tc_image(PotDevice& pd, const std::vector<double
 }
 
 int build_device_tables() {
+  ++g.gen;
   if (!cuda_ok()) return AENET_ERR_CUDA;
   PotDevice pd{};
   pd.ntypes = g.ntypes;
@@ -884,12 +887,23 @@ struct HostPlanCache {
   size_t io_bytes = 0;
   cudaStream_t stream = nullptr;
   unsigned* status_h = nullptr;   // pinned: the status read back stays asynchronous
+  // the plan's run captured as a CUDA graph (device pointers of the cached
+  // buffers are fixed), with the outputs it was captured for and g.gen
+  cudaGraphExec_t graph = nullptr;
+  unsigned graph_key = 0;
+  int graph_gen = -1;
   ~HostPlanCache() {
+    drop_graph();
     if (io) cudaFree(io);
     if (stream) cudaStreamDestroy(stream);
     if (status_h) cudaFreeHost(status_h);
   }
+  void drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
   void reset() {
+    drop_graph();
     plan.reset();
     if (io) cudaFree(io);
     io = nullptr;
@@ -1908,6 +1922,7 @@ EXPORT void aenet_nbl_neighbors(int iatom, int* nnb, double nbcoo[], double nbdi
 EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!key || !value) return AENET_ERR_INPUT;
+  ++g.gen;
   std::string k = key, v = value;
   if (k == "angular_domain") {
     if (v == "legacy") g.angular_legacy = 1;
@@ -2817,10 +2832,33 @@ int chunk_submit(HostPlanCache& c, int nstruc, const int* natoms, const double* 
     return AENET_ERR_CUDA;
   const unsigned flags =
       (want_forces ? AENET_GPU_FORCES : 0u) | (want_virial ? AENET_GPU_VIRIAL : 0u);
-  st = aenet_gpu_plan_run(P, d_c, d_t, d_E, want_E_atoms ? d_Ea : nullptr,
-                          (want_forces || want_virial) ? d_F : nullptr,
-                          want_virial ? d_V : nullptr, flags, s);
-  if (st) return st;
+  const unsigned key = flags | (want_E_atoms ? 4u : 0u);
+  if (!c.graph || c.graph_key != key || c.graph_gen != g.gen) {
+    // capture the run once per plan, outputs and settings; replays then
+    // cost one launch
+    c.drop_graph();
+    cudaGraph_t gr = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return AENET_ERR_CUDA;
+    st = aenet_gpu_plan_run(P, d_c, d_t, d_E, want_E_atoms ? d_Ea : nullptr,
+                            (want_forces || want_virial) ? d_F : nullptr,
+                            want_virial ? d_V : nullptr, flags, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+    if (st || ce != cudaSuccess || !gr) {
+      if (gr) cudaGraphDestroy(gr);
+      cudaGetLastError();
+      return st ? st : AENET_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c.graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ie != cudaSuccess) {
+      c.graph = nullptr;
+      return AENET_ERR_CUDA;
+    }
+    c.graph_key = key;
+    c.graph_gen = g.gen;
+  }
+  if (cudaGraphLaunch(c.graph, s) != cudaSuccess) return AENET_ERR_CUDA;
   return cudaMemcpyAsync(c.status_h, P->status, 4, cudaMemcpyDeviceToHost, s) ? AENET_ERR_CUDA : 0;
 }
 
