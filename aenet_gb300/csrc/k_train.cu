@@ -443,6 +443,354 @@ __global__ void __launch_bounds__(256) k_mlp_wgrad(PotDevice pd, WgradArgs A) {
   for (int q = threadIdx.x; q < A.wcap; q += blockDim.x) out[q] = q < lay.wsz ? (double)sdW[q] : 0.0;
 }
 
+// ---- tile form of the same pass: WT_TN atoms at a time, every layer as
+// register-blocked products over the tile.  Activations, tangents and node
+// adjoints are held feature-major ([feature][atom], rows WT_P apart) so
+// that four atoms of one feature are one vector load; each layer input
+// carries a row of ones (and its tangent a row of zeros), which makes the
+// bias an ordinary column.  Per layer l (nin -> nout):
+//   forward   z = W_l [X_l; 1], zd = W_l [Xd_l; 0]   (threads: 4 atoms x 2 nodes)
+//   reverse   dW_l += ZB_l [X_l; 1]^T + ZDB_l [Xd_l; 0]^T  (4 nodes x 4 inputs)
+//             ZB_{l-1} = f' (W_l^T ZB_l) + f'' zd (W_l^T ZDB_l),
+//             ZDB_{l-1} = f' (W_l^T ZDB_l)                 (4 atoms x 2 inputs)
+// The node adjoints of a hidden layer overwrite its f' and f'' zd rows,
+// which no other thread reads by then.  Padding atoms of the last tile
+// have zero inputs and zero coefficients, so they add nothing.
+constexpr int WT_TN = 32;           // atoms per tile
+constexpr int WT_P = WT_TN + 4;     // row pitch: 16-byte rows, successive rows 4 banks apart
+constexpr int WT_THREADS = 128;
+
+struct WtLayout {
+  int L;
+  int x[AE_MAXLAYERS];    // first row of [X_l; 1]            (nin_l + 1 rows)
+  int xd[AE_MAXLAYERS];   // first row of [Xd_l; 0]           (nin_l + 1 rows, tangents)
+  int s1[AE_MAXLAYERS];   // f' of the nodes of X_l, l >= 1   (nin_l rows) -> ZB_{l-1}
+  int s2[AE_MAXLAYERS];   // f'' zd of those nodes            (nin_l rows) -> ZDB_{l-1}
+  int out;                // output node: ZB, ZDB; energy coefficient per atom
+  int rows;
+  int wr[AE_MAXLAYERS];   // W_l row-major [nout][pr], bias at column nin
+  int pr[AE_MAXLAYERS];
+  int wt[AE_MAXLAYERS];   // W_l transposed [nin + 1][pt]
+  int pt[AE_MAXLAYERS];
+  int wend;               // end of both weight copies (elements)
+  int wsz;                // gradient in the device weight layout
+};
+
+__host__ __device__ inline WtLayout wt_layout(const NetTable& net, bool tang) {
+  WtLayout w{};
+  const int L = net.nlayers;
+  w.L = L;
+  int r = 0;
+  for (int l = 0; l + 1 < L; ++l) {
+    const int n = net.nnodes[l];
+    w.x[l] = r;
+    r += n + 1;
+    w.xd[l] = r;
+    if (tang) r += n + 1;
+    if (l >= 1) {
+      w.s1[l] = r;
+      r += n;
+      w.s2[l] = r;
+      if (tang) r += n;
+    }
+  }
+  w.out = r;
+  r += 3;
+  w.rows = r;
+  int e = r * WT_P;   // even: vector loads of weight pairs stay aligned
+  for (int l = 0; l + 1 < L; ++l) {
+    const int nin = net.nnodes[l], nout = net.nnodes[l + 1];
+    w.pr[l] = (nin + 2) & ~1;
+    w.pt[l] = (nout + 1) & ~1;
+    w.wr[l] = e;
+    e += nout * w.pr[l];
+    w.wt[l] = e;
+    e += (nin + 1) * w.pt[l];
+  }
+  w.wend = e;
+  w.wsz = net.w_off[L - 2] - net.w_off[0] + net.pitch[L - 2] * net.nnodes[L - 1];
+  return w;
+}
+
+template <typename T>
+__host__ __device__ inline size_t wt_smem_bytes(const WtLayout& w) {
+  return sizeof(T) * ((size_t)w.wend + w.wsz);
+}
+
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* p, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double (&v)[4]) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ void ld2(const float* p, float (&v)[2]) {
+  const float2 q = *reinterpret_cast<const float2*>(p);
+  v[0] = q.x; v[1] = q.y;
+}
+__device__ __forceinline__ void ld2(const double* p, double (&v)[2]) {
+  const double2 q = *reinterpret_cast<const double2*>(p);
+  v[0] = q.x; v[1] = q.y;
+}
+
+template <typename T, bool TANG>
+__global__ void __launch_bounds__(WT_THREADS) k_mlp_wgrad_tile(PotDevice pd, WgradArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int t = blockIdx.y;
+  const NetTable& net = pd.sp[t].net;
+  __shared__ WtLayout lay;   // indexed by layer at run time: keep it out of registers
+  if (threadIdx.x == 0) lay = wt_layout(net, TANG);
+  __syncthreads();
+  const int L = lay.L;
+  const int tid = threadIdx.x;
+  T* S = reinterpret_cast<T*>(smem_raw);
+  T* sdW = S + lay.wend;
+  const int wbeg = net.w_off[0];
+  const T* Wg = wsrc<T>(pd) + wbeg;
+  for (int q = tid; q < lay.wend + lay.wsz; q += WT_THREADS) S[q] = T(0);
+  __syncthreads();
+  for (int l = 0; l + 1 < L; ++l) {
+    const int nin = net.nnodes[l], nout = net.nnodes[l + 1], pitch = net.pitch[l];
+    const T* Wl = Wg + (net.w_off[l] - wbeg);
+    for (int q = tid; q < nout * (nin + 1); q += WT_THREADS) {
+      const int o = q / (nin + 1), k = q - o * (nin + 1);
+      const T v = Wl[o * pitch + k];
+      S[lay.wr[l] + o * lay.pr[l] + k] = v;
+      S[lay.wt[l] + k * lay.pt[l] + o] = v;
+    }
+    for (int r = tid; r < WT_P; r += WT_THREADS) S[(lay.x[l] + nin) * WT_P + r] = T(1);
+  }
+  const int beg = A.spec_off[t], nt = A.spec_off[t + 1] - beg;
+  const int per = (nt + gridDim.x - 1) / gridDim.x;
+  const int a0 = min(nt, blockIdx.x * per), a1 = min(nt, a0 + per);
+  const T kappa = A.physical ? T(pd.sp[t].E_scale) : T(1);
+  const int nsf_pad = pd.nsf_pad;
+  const int n0 = net.nnodes[0];
+  T* ZBo = S + lay.out * WT_P;
+  T* ZDBo = ZBo + WT_P;
+  T* CE = ZDBo + WT_P;
+  __syncthreads();
+
+  for (int tb = a0; tb < a1; tb += WT_TN) {
+    const int tn = min(WT_TN, a1 - tb);
+    // ---- inputs (zero rows past the tile's atoms) and energy coefficients
+    for (int q = tid; q < WT_TN * n0; q += WT_THREADS) {
+      const int r = q / n0, k = q - r * n0;
+      T g = T(0), v = T(0);
+      if (r < tn) {
+        const size_t i = (size_t)A.order[beg + tb + r];
+        g = reinterpret_cast<const T*>(A.G)[i * nsf_pad + k];
+        if (TANG) v = reinterpret_cast<const T*>(A.V)[i * nsf_pad + k];
+      }
+      S[(lay.x[0] + k) * WT_P + r] = g;
+      if (TANG) S[(lay.xd[0] + k) * WT_P + r] = v;
+    }
+    if (tid < WT_TN)
+      CE[tid] = tid < tn ? kappa * T(A.cE[A.atom_struct[A.order[beg + tb + tid]]]) : T(0);
+    __syncthreads();
+
+    // ---- forward through the hidden layers
+    for (int l = 0; l + 2 < L; ++l) {
+      const int nin = net.nnodes[l], nout = net.nnodes[l + 1], fa = net.f_a[l + 1];
+      const int items = (WT_TN / 4) * ((nout + 1) / 2);
+      for (int it = tid; it < items; it += WT_THREADS) {
+        const int r0 = 4 * (it % (WT_TN / 4)), o0 = 2 * (it / (WT_TN / 4));
+        T z[2][4], zd[2][4];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) z[j][e] = zd[j][e] = T(0);
+        const T* X = S + lay.x[l] * WT_P + r0;
+        const T* Xd = S + lay.xd[l] * WT_P + r0;
+        const T* Wt = S + lay.wt[l] + o0;
+        for (int k = 0; k <= nin; ++k) {
+          T x[4], w[2];
+          ld4(X + k * WT_P, x);
+          ld2(Wt + k * lay.pt[l], w);
+#pragma unroll
+          for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) z[j][e] = fma(w[j], x[e], z[j][e]);
+          if (TANG) {
+            T xd[4];
+            ld4(Xd + k * WT_P, xd);
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+              for (int e = 0; e < 4; ++e) zd[j][e] = fma(w[j], xd[e], zd[j][e]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int o = o0 + j;
+          if (o >= nout) break;
+          T y[4], d1[4], d2[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) activate2<T>(fa, z[j][e], y[e], d1[e], d2[e]);
+          st4(S + (lay.x[l + 1] + o) * WT_P + r0, y);
+          st4(S + (lay.s1[l + 1] + o) * WT_P + r0, d1);
+          if (TANG) {
+            T a[4], b[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              a[e] = d1[e] * zd[j][e];
+              b[e] = d2[e] * zd[j][e];
+            }
+            st4(S + (lay.xd[l + 1] + o) * WT_P + r0, a);
+            st4(S + (lay.s2[l + 1] + o) * WT_P + r0, b);
+          }
+        }
+      }
+      __syncthreads();
+    }
+
+    // ---- output node and its adjoints
+    {
+      const int l = L - 2, nin = net.nnodes[l];
+      if (tid < WT_TN) {
+        const T* X = S + lay.x[l] * WT_P + tid;
+        const T* Xd = S + lay.xd[l] * WT_P + tid;
+        const T* Wr = S + lay.wr[l];
+        T z = T(0), zd = T(0);
+        for (int k = 0; k <= nin; ++k) {
+          z = fma(Wr[k], X[k * WT_P], z);
+          if (TANG) zd = fma(Wr[k], Xd[k * WT_P], zd);
+        }
+        T y, d1, d2;
+        activate2<T>(net.f_a[L - 1], z, y, d1, d2);
+        const T ce = CE[tid];
+        const T cf = tid < tn ? kappa * T(A.cF) : T(0);
+        ZBo[tid] = TANG ? ce * d1 + cf * d2 * zd : ce * d1;
+        if (TANG) ZDBo[tid] = cf * d1;
+      }
+      __syncthreads();
+    }
+
+    // ---- reverse: weight gradients of layer l, then the adjoints of its inputs
+    for (int l = L - 2; l >= 0; --l) {
+      const int nin = net.nnodes[l], nout = net.nnodes[l + 1];
+      const T* ZB = l == L - 2 ? ZBo : S + lay.s1[l + 1] * WT_P;
+      const T* ZDB = l == L - 2 ? ZDBo : S + lay.s2[l + 1] * WT_P;
+      const T* X = S + lay.x[l] * WT_P;
+      const T* Xd = S + lay.xd[l] * WT_P;
+      {
+        const int kb = (nin + 1 + 3) / 4;
+        const int items = ((nout + 3) / 4) * kb;
+        T* dWl = sdW + (net.w_off[l] - wbeg);
+        for (int it = tid; it < items; it += WT_THREADS) {
+          const int o0 = 4 * (it / kb), k0 = 4 * (it % kb);
+          int orow[4], krow[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            orow[j] = min(o0 + j, nout - 1) * WT_P;
+            krow[j] = min(k0 + j, nin) * WT_P;
+          }
+          T acc[4][4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[j][c] = T(0);
+          for (int r = 0; r < WT_TN; r += 4) {
+            T x[4][4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) ld4(X + krow[c] + r, x[c]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              T zb[4];
+              ld4(ZB + orow[j] + r, zb);
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[j][c] = fma(zb[e], x[c][e], acc[j][c]);
+            }
+            if (TANG) {
+#pragma unroll
+              for (int c = 0; c < 4; ++c) ld4(Xd + krow[c] + r, x[c]);
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                T zb[4];
+                ld4(ZDB + orow[j] + r, zb);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+#pragma unroll
+                  for (int e = 0; e < 4; ++e) acc[j][c] = fma(zb[e], x[c][e], acc[j][c]);
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+              if (o0 + j < nout && k0 + c <= nin) dWl[(o0 + j) * net.pitch[l] + k0 + c] += acc[j][c];
+        }
+      }
+      if (l >= 1) {
+        // adjoints of the nodes of X_l, written over their f' / f'' zd rows
+        const int items = (WT_TN / 4) * ((nin + 1) / 2);
+        for (int it = tid; it < items; it += WT_THREADS) {
+          const int r0 = 4 * (it % (WT_TN / 4)), k0 = 2 * (it / (WT_TN / 4));
+          T ab[2][4], adb[2][4];
+#pragma unroll
+          for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) ab[j][e] = adb[j][e] = T(0);
+          const T* Wr = S + lay.wr[l] + k0;
+          for (int o = 0; o < nout; ++o) {
+            T zb[4], w[2];
+            ld4(ZB + o * WT_P + r0, zb);
+            ld2(Wr + o * lay.pr[l], w);
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+              for (int e = 0; e < 4; ++e) ab[j][e] = fma(w[j], zb[e], ab[j][e]);
+            if (TANG) {
+              ld4(ZDB + o * WT_P + r0, zb);
+#pragma unroll
+              for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) adb[j][e] = fma(w[j], zb[e], adb[j][e]);
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const int k = k0 + j;
+            if (k >= nin) break;
+            T* s1 = S + (lay.s1[l] + k) * WT_P + r0;
+            T* s2 = S + (lay.s2[l] + k) * WT_P + r0;
+            T d1[4], v[4];
+            ld4(s1, d1);
+            if (TANG) {
+              T d2z[4];
+              ld4(s2, d2z);
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                v[e] = d1[e] * ab[j][e] + d2z[e] * adb[j][e];
+                d2z[e] = d1[e] * adb[j][e];
+              }
+              st4(s2, d2z);
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e) v[e] = d1[e] * ab[j][e];
+            }
+            st4(s1, v);
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  double* out = A.partial + ((size_t)t * gridDim.x + blockIdx.x) * A.wcap;
+  for (int q = tid; q < A.wcap; q += WT_THREADS) out[q] = q < lay.wsz ? (double)sdW[q] : 0.0;
+}
+
 // sum the block partials (in block order) and write the gradient in the
 // reference's W order: per species, per layer, column-major (nout, nin+1)
 // with the bias in the last column (feedforward.f90:55-89)
@@ -548,7 +896,35 @@ int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_o
   A.physical = physical;
   A.partial = partial;
   A.wcap = ae_wgrad_wcap(pd);
-  // the largest tile whose shared memory fits every species
+  for (int t = 0; t < pd.ntypes; ++t)
+    if (pd.sp[t].net.nnodes[pd.sp[t].net.nlayers - 1] != 1 || pd.sp[t].net.nlayers < 2)
+      return (int)cudaErrorInvalidValue;
+  dim3 grid(nblk, pd.ntypes);
+  dim3 rgrid((A.wcap + 255) / 256, pd.ntypes);
+  // tile kernel when its shared memory fits every species
+  size_t tneed = 0;
+  for (int t = 0; t < pd.ntypes; ++t) {
+    const WtLayout w = wt_layout(pd.sp[t].net, tang);
+    const size_t b = fp64 ? wt_smem_bytes<double>(w) : wt_smem_bytes<float>(w);
+    tneed = tneed > b ? tneed : b;
+  }
+  if (tneed + AE_STATIC_SMEM <= 200 * 1024) {
+    auto go_tile = [&](auto kern) {
+      if (tneed + AE_STATIC_SMEM > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tneed);
+      kern<<<grid, WT_THREADS, tneed, s>>>(pd, A);
+    };
+    if (fp64) {
+      if (tang) go_tile(k_mlp_wgrad_tile<double, true>);
+      else go_tile(k_mlp_wgrad_tile<double, false>);
+    } else {
+      if (tang) go_tile(k_mlp_wgrad_tile<float, true>);
+      else go_tile(k_mlp_wgrad_tile<float, false>);
+    }
+    k_wgrad_reduce<<<rgrid, 256, 0, s>>>(pd, nblk, A.wcap, partial, grad);
+    return (int)cudaGetLastError();
+  }
+  // otherwise one warp per atom: the largest tile whose shared memory fits
   size_t need = 0;
   int tile = 32;
   for (; tile >= 4; tile /= 2) {
@@ -562,10 +938,6 @@ int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_o
   }
   if (tile < 4) return (int)cudaErrorInvalidValue;
   A.tile = tile;
-  for (int t = 0; t < pd.ntypes; ++t)
-    if (pd.sp[t].net.nnodes[pd.sp[t].net.nlayers - 1] != 1 || pd.sp[t].net.nlayers < 2)
-      return (int)cudaErrorInvalidValue;
-  dim3 grid(nblk, pd.ntypes);
   auto go = [&](auto kern) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
     kern<<<grid, warps * 32, need, s>>>(pd, A);
@@ -577,7 +949,6 @@ int ae_launch_mlp_wgrad(const PotDevice& pd, const int* order, const int* spec_o
     if (tang) go(k_mlp_wgrad<float, true>);
     else go(k_mlp_wgrad<float, false>);
   }
-  dim3 rgrid((A.wcap + 255) / 256, pd.ntypes);
   k_wgrad_reduce<<<rgrid, 256, 0, s>>>(pd, nblk, A.wcap, partial, grad);
   return (int)cudaGetLastError();
 }
