@@ -459,6 +459,8 @@ __global__ void __launch_bounds__(256) k_mlp_wgrad(PotDevice pd, WgradArgs A) {
 constexpr int WT_TN = 32;           // atoms per tile
 constexpr int WT_P = WT_TN + 4;     // row pitch: 16-byte rows, successive rows 4 banks apart
 constexpr int WT_THREADS = 128;
+static_assert(WT_THREADS == 4 * WT_TN, "the output node takes four threads per atom");
+constexpr int WT_PF = 8;            // inputs per thread and array held for the next tile
 
 struct WtLayout {
   int L;
@@ -542,7 +544,7 @@ __device__ __forceinline__ void ld2(const double* p, double (&v)[2]) {
 }
 
 template <typename T, bool TANG>
-__global__ void __launch_bounds__(WT_THREADS) k_mlp_wgrad_tile(PotDevice pd, WgradArgs A) {
+__global__ void __launch_bounds__(WT_THREADS, 3) k_mlp_wgrad_tile(PotDevice pd, WgradArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = blockIdx.y;
   const NetTable& net = pd.sp[t].net;
@@ -577,24 +579,58 @@ __global__ void __launch_bounds__(WT_THREADS) k_mlp_wgrad_tile(PotDevice pd, Wgr
   T* ZBo = S + lay.out * WT_P;
   T* ZDBo = ZBo + WT_P;
   T* CE = ZDBo + WT_P;
+  const T* Gin = reinterpret_cast<const T*>(A.G);
+  const T* Vin = reinterpret_cast<const T*>(A.V);
+  // inputs of a tile (zero rows past its atoms) and the energy coefficients;
+  // with few enough features the next tile's are loaded into registers
+  // while the current tile is processed
+  const bool pf = WT_TN * n0 <= WT_PF * WT_THREADS;
+  T pg[WT_PF], pv[WT_PF], pce = T(0);
+  auto fetch = [&](int tb1) {
+    const int tn1 = min(WT_TN, a1 - tb1);
+#pragma unroll
+    for (int j = 0; j < WT_PF; ++j) {
+      const int q = tid + j * WT_THREADS, r = q / n0, k = q - r * n0;
+      pg[j] = pv[j] = T(0);
+      if (q < WT_TN * n0 && r < tn1) {
+        const size_t i = (size_t)A.order[beg + tb1 + r];
+        pg[j] = Gin[i * nsf_pad + k];
+        if (TANG) pv[j] = Vin[i * nsf_pad + k];
+      }
+    }
+    if (tid < WT_TN) pce = tid < tn1 ? kappa * T(A.cE[A.atom_struct[A.order[beg + tb1 + tid]]]) : T(0);
+  };
+  if (pf && a0 < a1) fetch(a0);
   __syncthreads();
 
   for (int tb = a0; tb < a1; tb += WT_TN) {
     const int tn = min(WT_TN, a1 - tb);
-    // ---- inputs (zero rows past the tile's atoms) and energy coefficients
-    for (int q = tid; q < WT_TN * n0; q += WT_THREADS) {
-      const int r = q / n0, k = q - r * n0;
-      T g = T(0), v = T(0);
-      if (r < tn) {
-        const size_t i = (size_t)A.order[beg + tb + r];
-        g = reinterpret_cast<const T*>(A.G)[i * nsf_pad + k];
-        if (TANG) v = reinterpret_cast<const T*>(A.V)[i * nsf_pad + k];
+    if (pf) {
+#pragma unroll
+      for (int j = 0; j < WT_PF; ++j) {
+        const int q = tid + j * WT_THREADS, r = q / n0, k = q - r * n0;
+        if (q < WT_TN * n0) {
+          S[(lay.x[0] + k) * WT_P + r] = pg[j];
+          if (TANG) S[(lay.xd[0] + k) * WT_P + r] = pv[j];
+        }
       }
-      S[(lay.x[0] + k) * WT_P + r] = g;
-      if (TANG) S[(lay.xd[0] + k) * WT_P + r] = v;
+      if (tid < WT_TN) CE[tid] = pce;
+      if (tb + WT_TN < a1) fetch(tb + WT_TN);
+    } else {
+      for (int q = tid; q < WT_TN * n0; q += WT_THREADS) {
+        const int r = q / n0, k = q - r * n0;
+        T g = T(0), v = T(0);
+        if (r < tn) {
+          const size_t i = (size_t)A.order[beg + tb + r];
+          g = Gin[i * nsf_pad + k];
+          if (TANG) v = Vin[i * nsf_pad + k];
+        }
+        S[(lay.x[0] + k) * WT_P + r] = g;
+        if (TANG) S[(lay.xd[0] + k) * WT_P + r] = v;
+      }
+      if (tid < WT_TN)
+        CE[tid] = tid < tn ? kappa * T(A.cE[A.atom_struct[A.order[beg + tb + tid]]]) : T(0);
     }
-    if (tid < WT_TN)
-      CE[tid] = tid < tn ? kappa * T(A.cE[A.atom_struct[A.order[beg + tb + tid]]]) : T(0);
     __syncthreads();
 
     // ---- forward through the hidden layers
@@ -652,24 +688,30 @@ __global__ void __launch_bounds__(WT_THREADS) k_mlp_wgrad_tile(PotDevice pd, Wgr
       __syncthreads();
     }
 
-    // ---- output node and its adjoints
+    // ---- output node and its adjoints: four threads per atom
     {
       const int l = L - 2, nin = net.nnodes[l];
-      if (tid < WT_TN) {
-        const T* X = S + lay.x[l] * WT_P + tid;
-        const T* Xd = S + lay.xd[l] * WT_P + tid;
-        const T* Wr = S + lay.wr[l];
-        T z = T(0), zd = T(0);
-        for (int k = 0; k <= nin; ++k) {
-          z = fma(Wr[k], X[k * WT_P], z);
-          if (TANG) zd = fma(Wr[k], Xd[k * WT_P], zd);
-        }
+      const int r = tid >> 2, part = tid & 3;
+      const T* X = S + lay.x[l] * WT_P + r;
+      const T* Xd = S + lay.xd[l] * WT_P + r;
+      const T* Wr = S + lay.wr[l];
+      T z = T(0), zd = T(0);
+      for (int k = part; k <= nin; k += 4) {
+        z = fma(Wr[k], X[k * WT_P], z);
+        if (TANG) zd = fma(Wr[k], Xd[k * WT_P], zd);
+      }
+#pragma unroll
+      for (int d = 1; d < 4; d <<= 1) {
+        z += __shfl_xor_sync(0xffffffffu, z, d);
+        if (TANG) zd += __shfl_xor_sync(0xffffffffu, zd, d);
+      }
+      if (part == 0) {
         T y, d1, d2;
         activate2<T>(net.f_a[L - 1], z, y, d1, d2);
-        const T ce = CE[tid];
-        const T cf = tid < tn ? kappa * T(A.cF) : T(0);
-        ZBo[tid] = TANG ? ce * d1 + cf * d2 * zd : ce * d1;
-        if (TANG) ZDBo[tid] = cf * d1;
+        const T ce = CE[r];
+        const T cf = r < tn ? kappa * T(A.cF) : T(0);
+        ZBo[r] = TANG ? ce * d1 + cf * d2 * zd : ce * d1;
+        if (TANG) ZDBo[r] = cf * d1;
       }
       __syncthreads();
     }
@@ -682,22 +724,25 @@ __global__ void __launch_bounds__(WT_THREADS) k_mlp_wgrad_tile(PotDevice pd, Wgr
       const T* X = S + lay.x[l] * WT_P;
       const T* Xd = S + lay.xd[l] * WT_P;
       {
-        const int kb = (nin + 1 + 3) / 4;
-        const int items = ((nout + 3) / 4) * kb;
+        // 4 nodes x 4 inputs per thread; the inputs of one thread are kn
+        // apart so that neighbouring lanes read neighbouring rows (banks)
+        const int kn = (nin + 1 + 3) / 4;
+        const int items = ((nout + 3) / 4) * kn;
         T* dWl = sdW + (net.w_off[l] - wbeg);
         for (int it = tid; it < items; it += WT_THREADS) {
-          const int o0 = 4 * (it / kb), k0 = 4 * (it % kb);
+          const int o0 = 4 * (it / kn), k0 = it % kn;
           int orow[4], krow[4];
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
             orow[j] = min(o0 + j, nout - 1) * WT_P;
-            krow[j] = min(k0 + j, nin) * WT_P;
+            krow[j] = min(k0 + j * kn, nin) * WT_P;
           }
           T acc[4][4];
 #pragma unroll
           for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int c = 0; c < 4; ++c) acc[j][c] = T(0);
+#pragma unroll 2
           for (int r = 0; r < WT_TN; r += 4) {
             T x[4][4];
 #pragma unroll
@@ -729,7 +774,8 @@ __global__ void __launch_bounds__(WT_THREADS) k_mlp_wgrad_tile(PotDevice pd, Wgr
           for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int c = 0; c < 4; ++c)
-              if (o0 + j < nout && k0 + c <= nin) dWl[(o0 + j) * net.pitch[l] + k0 + c] += acc[j][c];
+              if (o0 + j < nout && k0 + c * kn <= nin)
+                dWl[(o0 + j) * net.pitch[l] + k0 + c * kn] += acc[j][c];
         }
       }
       if (l >= 1) {
