@@ -224,8 +224,15 @@ __global__ void __launch_bounds__(128) k_tangent(PotDevice pd, DescBuffers b) {
 // D_e Y_lm from the recurrences: d/dz Q_l^m = kap Q_l^{m+1} and
 // d (x + i y)^m = m (x + i y)^{m-1} (e_x + i e_y).  Each lane contracts its
 // neighbours' terms with M at once, so only 2 (A + 1) sums cross lanes.
+// resident blocks per SM asked of the register allocator (angular degree
+// up to 4; the degree-6 instance would spill under the same cap and keeps
+// three)
+#ifndef AE_TAN_MOM_BLOCKS
+#define AE_TAN_MOM_BLOCKS 5
+#endif
+
 template <int R, int A, int LPA>
-__global__ void __launch_bounds__(128) k_tangent_mom(PotDevice pd, DescBuffers b) {
+__global__ void __launch_bounds__(128, A <= 5 ? AE_TAN_MOM_BLOCKS : 3) k_tangent_mom(PotDevice pd, DescBuffers b) {
   using T = float;
   using T4 = float4;
   constexpr int L = A - 1;
