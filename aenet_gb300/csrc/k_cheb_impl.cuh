@@ -316,10 +316,13 @@ __device__ __forceinline__ void forward_moments(const PotDevice& pd, const DescB
 #ifndef AE_MOM_ADJ_BLOCKS
 #define AE_MOM_ADJ_BLOCKS 5
 #endif
+#ifndef AE_PAIR_ADJ_BLOCKS
+#define AE_PAIR_ADJ_BLOCKS 5
+#endif
 
 template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
-__global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(PotDevice pd,
-                                                                             DescBuffers b) {
+__global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_FWD_BLOCKS : 3) : 1)
+    k_forward(PotDevice pd, DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
   extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -513,8 +516,12 @@ __global__ void __launch_bounds__(128, MOM ? AE_MOM_FWD_BLOCKS : 1) k_forward(Po
 // ----------------------------------------------------------------------
 // adjoint
 // ----------------------------------------------------------------------
+// FP32 pair form of the exact-size instances: five blocks as well; the
+// moment form of degree 6 keeps three (its sums would spill under more)
 template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
-__global__ void __launch_bounds__(128, MOM ? AE_MOM_ADJ_BLOCKS : 1) k_adjoint(PotDevice pd,
+__global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_ADJ_BLOCKS : 3)
+                                           : (sizeof(T) == 4 && !GUARD ? AE_PAIR_ADJ_BLOCKS : 1))
+    k_adjoint(PotDevice pd,
                                                                              DescBuffers b) {
   using T4 = typename Vec4<T>::type;
   constexpr int GPW = 32 / LPA;
