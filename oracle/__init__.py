@@ -1,8 +1,8 @@
 """FP64 CPU oracle for aenet's energy-and-force path -- TEST INFRASTRUCTURE.
 
 Only the test suite, ``__graft_entry__.smoke()`` and the benchmark's CPU
-baseline leg import this package, and only as the checker: the product
-library never loads it.  The numerics live in ``aenet_oracle.c`` (a plain-C
+baseline leg import this package, and only to check or time against: the
+product library never loads it.  The numerics live in ``aenet_oracle.c`` (a plain-C
 restatement of the reference Fortran, built by ``oracle/build.py``); this
 module is a thin ctypes front end.
 
