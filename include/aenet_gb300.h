@@ -46,6 +46,8 @@ extern "C" {
  *       finely to the cut-off sphere (performance only).
  *   "lanes_per_atom" = "8" | "16" | "32"   descriptor kernels' lanes per
  *       atom (performance only).
+ *   "adjoint_lanes_per_atom" = "0" | "8" | "16" | "32"   the same for the
+ *       adjoint kernels; 0 follows lanes_per_atom (performance only).
  *   "neighbour_kernel" = "atom" | "cell" | "stream" | "half"   neighbour
  *       search with one warp per atom (pruned per atom), one warp per home
  *       cell with a lane per home atom (dense cells of large structures),
@@ -62,8 +64,9 @@ extern "C" {
  *       sum rewritten by the addition theorem; cost linear in the angular
  *       neighbours, angular orders up to 6) or from the pair sum itself.
  *       Same values up to FP32 rounding; the FP64 path always sums pairs.
- * Returns AENET_OK or AENET_ERR_INPUT.  Takes effect at the next load or
- * plan creation. */
+ * Returns AENET_OK or AENET_ERR_INPUT.  "cell_div" and "z_refine" apply to
+ * plans created afterwards, "angular_domain" from the next evaluation (the
+ * device tables are rebuilt), the others from the next launch. */
 int aenet_gpu_set_option(const char* key, const char* value);
 
 /* Energy and forces of one structure from HOST arrays.  Replaces the atom
