@@ -42,6 +42,26 @@ def batch(oracle, tmp_path_factory):
     return w, paths, tpaths
 
 
+@pytest.fixture(scope="module")
+def batch_odd(oracle, tmp_path_factory):
+    """The same eight cells under a 40-feature descriptor (radial order 12,
+    angular order 6) and 40-25-25-1 networks: odd layer widths, and more
+    inputs than the weight-gradient kernel stages ahead in registers."""
+    from aenet_gb300 import workloads
+    base = workloads.lisio_batch_4096(nstruc=8)
+    arch = [40, 25, 25, 1]
+    w = workloads.Workload("lisio_odd", base.types,
+                           workloads.cheb_setups(base.types, 12, 6.0, 6, 4.0), arch,
+                           base.structures, base.seed)
+    w.networks = workloads.glorot_networks(np.random.default_rng(5), w.types, arch)
+    d = tmp_path_factory.mktemp("train_odd")
+    paths = helpers.make_potentials(oracle, w, str(d))
+    teacher = workloads.glorot_networks(np.random.default_rng(105), w.types, arch)
+    tpaths = workloads.write_potentials(w, str(d / "teacher"), stats=_stats_of(paths, w),
+                                        networks=teacher)
+    return w, paths, tpaths
+
+
 def _stats_of(paths, w):
     from aenet_gb300.nnfile import read_nn
     out = {}
@@ -70,11 +90,12 @@ def _targets(w, tpaths):
     return r["energy"], r["forces"]
 
 
-def test_energy_loss_gradient_matches_oracle(cuda, oracle, batch):
+@pytest.mark.parametrize("which", ["batch", "batch_odd"])
+def test_energy_loss_gradient_matches_oracle(cuda, oracle, request, which):
     from aenet_gb300 import workloads
     from aenet_gb300.core import FP64
     from aenet_gb300.train import LOSS_ENERGY, Trainer
-    w, paths, tpaths = batch
+    w, paths, tpaths = request.getfixturevalue(which)
     E_t, _ = _targets(w, tpaths)
     ann = _ann(paths, w.types)
     try:
@@ -112,10 +133,11 @@ def test_energy_loss_gradient_matches_oracle(cuda, oracle, batch):
     assert np.abs(g - ref).max() <= G_REL_FP64 * np.abs(ref).max()
 
 
-def test_force_loss_gradient_matches_finite_differences(cuda, batch):
+@pytest.mark.parametrize("which", ["batch", "batch_odd"])
+def test_force_loss_gradient_matches_finite_differences(cuda, request, which):
     from aenet_gb300.core import FP64
     from aenet_gb300.train import LOSS_ENERGY_FORCES, Trainer
-    w, paths, tpaths = batch
+    w, paths, tpaths = request.getfixturevalue(which)
     E_t, F_t = _targets(w, tpaths)
     ann = _ann(paths, w.types)
     try:
@@ -126,11 +148,13 @@ def test_force_loss_gradient_matches_finite_differences(cuda, batch):
         nws = [ann.nweights(t) for t in w.types]
         offs = np.concatenate([[0], np.cumsum(nws)])
         # per species: a first-layer weight, a first-layer bias, a hidden
-        # weight and the output bias
+        # weight and the output bias (W per layer column-major (nout, nin+1),
+        # bias in the last column)
+        n0, n1 = w.arch[0], w.arch[1]
         picks = []
         for t in range(len(w.types)):
             o = offs[t]
-            picks += [o + 5, o + 32 * 32 + 7, o + 33 * 32 + 40, offs[t + 1] - 1]
+            picks += [o + 5, o + n1 * n0 + 7, o + (n0 + 1) * n1 + 40, offs[t + 1] - 1]
         for k in picks:
             h = 1e-4 * max(1.0, abs(W0[k]))
             f = {}
@@ -146,10 +170,11 @@ def test_force_loss_gradient_matches_finite_differences(cuda, batch):
         ann.release()
 
 
-def test_mixed_gradient_close_to_fp64(cuda, batch):
+@pytest.mark.parametrize("which", ["batch", "batch_odd"])
+def test_mixed_gradient_close_to_fp64(cuda, request, which):
     from aenet_gb300.core import FP64, MIXED
     from aenet_gb300.train import LOSS_ENERGY_FORCES, Trainer
-    w, paths, tpaths = batch
+    w, paths, tpaths = request.getfixturevalue(which)
     E_t, F_t = _targets(w, tpaths)
     ann = _ann(paths, w.types)
     try:
