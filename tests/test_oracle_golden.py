@@ -181,3 +181,44 @@ def test_k5_fcc_neighbour_count_and_rotation_invariance(oracle, tmp_path):
     e0 = oracle.structure(s.cell, s.positions, s.types, forces=False)[1]
     e1 = oracle.structure(s.cell @ q, s.positions @ q, s.types, forces=False)[1]
     assert abs(e1 - e0) / s.natoms < 1e-10
+
+
+@pytest.mark.parametrize("which", ["behler", "chebyshev"])
+def test_oracle_descriptor_derivatives_match_finite_differences(oracle, tmp_path, which):
+    """The oracle's raw descriptor derivatives (what the GPU Jacobian export
+    is checked against) against central differences of its descriptors,
+    with respect to the central atom and to single neighbours: Behler
+    G2/G4 (symmfunc, rutile Ti/O) and the species-weighted Chebyshev basis
+    (sfbasis, Li/Si/O)."""
+    from aenet_gb300 import workloads
+    from tests import helpers
+    if which == "behler":
+        w = workloads.tio2_rutile_9000(cells=(1, 1, 2))
+    else:
+        w = workloads.lisio_batch_4096(nstruc=2)
+    s = w.structures[0]
+    paths = helpers.make_potentials(oracle, w, str(tmp_path), max_atoms=64)
+    oracle.load(w.types, paths)
+    _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types, atoms=[0, 1])
+    h = 1e-5
+    for a in (0, 1):
+        nbcoo, _, _, nbt = nb[a]
+        ti = int(s.types[a])
+
+        def G(ci, cj):
+            return oracle.descriptor(ci, ti, cj, nbt, scaled=False)
+
+        G0, di, dj = oracle.descriptor(centres[a], ti, nbcoo, nbt, scaled=False, deriv=True)
+        tol = 1e-6 * max(1.0, np.abs(di).max(), np.abs(dj).max())
+        for c in range(3):
+            e = np.zeros(3)
+            e[c] = h
+            fd = (G(centres[a] + e, nbcoo) - G(centres[a] - e, nbcoo)) / (2 * h)
+            assert np.abs(fd - di[:, c]).max() <= tol, (a, c)
+        for j in (0, len(nbt) // 2, len(nbt) - 1):
+            for c in range(3):
+                cp, cm = nbcoo.copy(), nbcoo.copy()
+                cp[j, c] += h
+                cm[j, c] -= h
+                fd = (G(centres[a], cp) - G(centres[a], cm)) / (2 * h)
+                assert np.abs(fd - dj[j, :, c]).max() <= tol, (a, j, c)
