@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--no-md", action="store_true", help="skip the 1M-atom MD leg")
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the single-structure configurations (256, 4000, 9000, 1M atoms)")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "aenet_gb300_bench"))
     return ap.parse_args()
 
@@ -523,12 +525,13 @@ def run_gb300(args):
                  "loss": float(lbuf.item())}
         plan_t.close()
 
+    ann.release()
+    configs = None
+    if rank == 0 and not args.no_configs:
+        configs = run_configs(args, local, flush, peak.value)
     md = None
     if rank == 0 and not args.no_md:
-        ann.release()
         md = run_md(args, local)
-    else:
-        ann.release()
 
     launches_per_step = 16   # types, 6 neighbour-search kernels, descriptor, 3 species-
     #                          partition kernels, tensor-core networks, 2 energy-reduction
@@ -546,17 +549,157 @@ def run_gb300(args):
                            "parallelism": "replicas" if world > 1 else "single GPU",
                            "cuda_graph": not args.no_graph,
                            "angular_terms": args.angular_terms,
-                           "launch_shape": tuned},
+                           "launch_shape": {k: v for k, v in (tuned or {}).items()
+                                            if k != "all"}},
+                "configs": configs, "md": md, "train_step": train,
+                "neighbours": nb, "stages_ms": stages, "roofline": roof, "cpu_baseline": cpu,
+                "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+                "wall_s_timed_region": wall,
+                # the metric's own comparison last, so that it ends the line
                 "fp64": {"value": value64, "unit": "atoms/s", "ms_per_step": ms64},
-                "mixed_over_fp64": value / value64,
-                "errors_vs_fp64": errors, "neighbours": nb,
-                "stages_ms": stages, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-                "train_step": train, "md": md,
-                "wall_s_timed_region": wall}
+                "errors_vs_fp64": errors, "mixed_over_fp64": value / value64}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def behler_counts(plan, rc):
+    """n (neighbours within rc) and P3 (pairs j < k of them with r_jk < rc
+    too) per atom, averaged, from the plan's neighbour table."""
+    import torch
+    cap, cnt, jt, vec = plan.neighbors()
+    n_tot, p3_tot = 0.0, 0.0
+    for a0 in range(0, plan.natoms, 1024):
+        v = vec[a0:a0 + 1024].double()
+        c = cnt[a0:a0 + 1024].long()
+        ok = (torch.arange(cap, device=v.device)[None, :] < c[:, None]) & (v[..., 3] < rc) \
+            & (v[..., 3] > 1e-8)
+        n_tot += ok.sum().item()
+        R = v[..., :3]
+        d = torch.cdist(R, R)
+        m = ok[:, :, None] & ok[:, None, :] & (d < rc)
+        p3_tot += (torch.triu(m, diagonal=1)).sum().item()
+    return n_tot / plan.natoms, p3_tot / plan.natoms
+
+
+def behler_flops(n, P3, g2, g4, nsf):
+    """Canonical flops per atom of the G2/G4 forward and adjoint."""
+    fwd = n * (14 + 10 * g2) + P3 * (30 + 16 * g4) + 2 * nsf
+    adj = n * (9 + 8 * g2) + P3 * (40 + 40 * g4)
+    return fwd, adj
+
+
+def time_cpu(o, s, threads, seconds):
+    """atoms/s of the oracle's predict.x loop on `threads` host threads over
+    the first atoms of structure s (sized to about `seconds`)."""
+    probe = min(s.natoms, 16 * threads)
+    t0 = time.perf_counter()
+    o.structure(s.cell, s.positions, s.types, nthreads=threads, atom_limit=probe)
+    dt = time.perf_counter() - t0
+    k = int(min(s.natoms, max(probe, probe * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    o.structure(s.cell, s.positions, s.types, nthreads=threads, atom_limit=k)
+    dt = time.perf_counter() - t0
+    return k / dt, k
+
+
+def run_configs(args, local, flush, fp32_peak):
+    """Energy and forces of the single-structure configurations, FP64 and
+    mixed, device-timed (CUDA graph replays, L2 flushed between steps), the
+    mixed path's error against FP64, and the oracle port of the reference's
+    predict.x loop on 1 host thread and on all of them."""
+    import torch
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import ANNPotentials, FP64, MIXED
+    from aenet_gb300.plan import Plan
+    from oracle import Oracle
+    stream = torch.cuda.current_stream()
+    dev = torch.device("cuda", local)
+    threads = os.cpu_count() or 1
+    out = {}
+    for name in ("cu_fcc_256", "aucu_fcc_4000", "tio2_rutile_9000", "cuau_fcc_1m"):
+        w = workloads.WORKLOADS[name]()
+        s = w.structures[0]
+        d = tempfile.mkdtemp(prefix="aenet_cfg_")
+        paths = workloads.write_potentials(w, d, workloads.gpu_descriptor_fn,
+                                           max_atoms_for_stats=4000)
+        ann = ANNPotentials(paths)
+        behler = name.startswith("tio2")
+        row = {"atoms": s.natoms}
+        try:
+            p = torch.tensor(s.positions, device=dev)
+            t = torch.tensor(s.types, device=dev)
+            res = {}
+            for prec, key in ((FP64, "fp64"), (MIXED, "mixed")):
+                plan = Plan([s.natoms], s.cell[None], [1], precision=prec, coords0=s.positions)
+                o = plan.run(p, t, virial=behler)
+                plan.check()
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph):
+                    plan.run(p, t, virial=behler, out=o)
+                for _ in range(3):
+                    graph.replay()
+                reps = 5 if s.natoms > 100000 or (behler and prec == FP64) else 20
+                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                      for _ in range(reps)]
+                torch.cuda.synchronize()
+                for k in range(reps):
+                    flush.zero_()
+                    ev[k][0].record(stream)
+                    graph.replay()
+                    ev[k][1].record(stream)
+                torch.cuda.synchronize()
+                ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+                plan.check()
+                res[key] = {k2: v.clone() for k2, v in o.items()}
+                row[key] = {"atoms_per_s": s.natoms / (ms * 1e-3), "ms": ms}
+                if behler:
+                    st = {}
+                    for _ in range(3):
+                        for k2, v in plan.profile(p, t).items():
+                            st[k2] = st.get(k2, 0.0) + v / 3
+                    row[key]["stages_ms"] = {k2: round(v, 4) for k2, v in st.items()}
+                    if prec == FP64:
+                        n_b, p3 = behler_counts(plan, 6.5)
+                        nsf = w.setups[w.types[0]]["nsf"]
+                        fwd, adj = behler_flops(n_b, p3, 8, 16, nsf)
+                        row["behler"] = {"n": n_b, "P3": p3, "flops_fwd_per_atom": fwd,
+                                         "flops_adj_per_atom": adj}
+                del graph
+                plan.close()
+            dE = abs(res["mixed"]["E"] - res["fp64"]["E"]).item() / s.natoms
+            dF = res["mixed"]["F"] - res["fp64"]["F"]
+            row["mixed_over_fp64"] = row["mixed"]["atoms_per_s"] / row["fp64"]["atoms_per_s"]
+            row["errors_vs_fp64"] = {"energy_eV_per_atom": dE,
+                                     "force_rms_eV_per_A": dF.pow(2).mean().sqrt().item(),
+                                     "force_max_eV_per_A": dF.abs().max().item()}
+            if behler:
+                b = row["behler"]
+                for key in ("fp64", "mixed"):
+                    stg = row[key]["stages_ms"]
+                    b[key + "_tflops_fwd"] = b["flops_fwd_per_atom"] * s.natoms / (
+                        stg["descriptor"] * 1e-3) / 1e12
+                    b[key + "_tflops_adj"] = b["flops_adj_per_atom"] * s.natoms / (
+                        stg["adjoint"] * 1e-3) / 1e12
+                if fp32_peak:
+                    b["fp32_peak_tflops"] = fp32_peak
+                    b["mixed_frac_fwd"] = b["mixed_tflops_fwd"] / fp32_peak
+                    b["mixed_frac_adj"] = b["mixed_tflops_adj"] / fp32_peak
+        finally:
+            ann.release()
+        if not args.no_cpu:
+            o = Oracle()
+            o.load(w.types, paths)
+            o.set_candidates("cells")
+            r1, k1 = time_cpu(o, s, 1, args.cpu_seconds / 8)
+            ra, ka = time_cpu(o, s, threads, args.cpu_seconds / 8)
+            o.close()
+            row["cpu"] = {"1_thread": r1, "all_threads": ra, "threads": threads,
+                          "sample_atoms": [k1, ka],
+                          "kind": "port (FP64 oracle, predict.x loop, linked-cell search)"}
+            row["mixed_over_cpu_all"] = row["mixed"]["atoms_per_s"] / ra
+        out[name] = row
+    return out
 
 
 def run_md(args, local):
@@ -604,7 +747,7 @@ def run_md(args, local):
                "energy_drift_max_eV_per_atom": max(drift),
                "timing": "host wall clock around md.run blocks of 10 steps (one sync per "
                          "step for the skin check), FP64 monitor outside",
-               "launch_shape": tuned}
+               "launch_shape": {k: v for k, v in (tuned or {}).items() if k != "all"}}
         md.close()
     finally:
         ann.release()

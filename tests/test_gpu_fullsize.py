@@ -143,3 +143,62 @@ def test_cuau_fcc_1m_full_size(cuda, oracle, tmp_path):
     dF = r32["forces"] - F64
     assert np.sqrt(np.mean(dF ** 2)) < F_RMS_MIXED
     assert np.abs(dF).max() < 10 * F_RMS_MIXED
+
+
+def test_tio2_rutile_9000_full_size(cuda, oracle, tmp_path):
+    """The Behler-Parrinello configuration at its stated size: rutile Ti/O
+    10x10x15 unit cells (9000 atoms), 8 G2 per pair and 16 G4 per triple
+    (64 features), Rc 6.5 A, 64-30-30-1 networks.  FP64 energies and
+    forces of every atom against the oracle (the whole structure, the
+    reference's per-atom loop on all host cores); the FP64 virial against
+    central differences of the FP64 energy under strain; the mixed path
+    within 1 meV/atom and 20 meV/A RMS of FP64."""
+    import os
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import ANNPotentials, FP64, MIXED
+    w = workloads.tio2_rutile_9000()
+    s = w.structures[0]
+    assert s.natoms == 9000
+    paths = helpers.make_potentials(oracle, w, str(tmp_path), max_atoms=600)
+    ann = ANNPotentials({t: paths[t] for t in w.types})
+    try:
+        r64 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64,
+                                          virial=True)
+        r32 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=MIXED,
+                                          virial=True)
+        h = 1e-5
+        W = np.zeros((3, 3))
+        for a in range(3):
+            for b in range(3):
+                E = []
+                for sgn in (-1, 1):
+                    eps = np.eye(3)
+                    eps[a, b] += sgn * h
+                    E.append(ann.structure_energy_forces(s.positions @ eps, s.types,
+                                                         s.cell @ eps, precision=FP64,
+                                                         forces=False)["energy"])
+                W[a, b] = -(E[1] - E[0]) / (2 * h)
+    finally:
+        ann.release()
+    n = s.natoms
+    oracle.load(w.types, paths)
+    oracle.set_candidates("cells")
+    try:
+        ec, et, F, Ea = oracle.structure(s.cell, s.positions, s.types,
+                                         nthreads=os.cpu_count() or 1)
+    finally:
+        oracle.set_candidates("complete")
+    assert abs(r64["energy"] - et) / n < E_TOL_FP64
+    assert np.abs(r64["atomic_energies"] - Ea).max() < E_TOL_FP64
+    assert np.abs(r64["forces"] - F).max() < F_TOL_FP64
+    F64 = r64["forces"]
+    assert np.abs(F64.sum(axis=0)).max() < _force_sum_tol(n, F64)
+    # central differences of an energy of ~-2e4 eV at h = 1e-5: ~1e-6 relative
+    assert np.abs(r64["virial"] - W).max() < 1e-5 * max(1.0, np.abs(W).max())
+    assert np.abs(W - W.T).max() <= 1e-5 * max(1.0, np.abs(W).max())
+    assert abs(r32["energy"] - r64["energy"]) / n < E_TOL_MIXED
+    dF = r32["forces"] - F64
+    assert np.sqrt(np.mean(dF ** 2)) < F_RMS_MIXED
+    assert np.abs(dF).max() < 10 * F_RMS_MIXED
+    dV = r32["virial"] - r64["virial"]
+    assert np.abs(dV).max() < 1e-3 * max(1.0, np.abs(r64["virial"]).max())

@@ -364,8 +364,37 @@ def test_capacity_overflow_is_reported_and_retried(cuda, cu256):
         ann.release()
 
 
+def _neighbour_keys(torch, plan, pos, cells, nat):
+    """Per-row sorted keys (neighbour index, lattice image) of a plan's
+    table.  The image n of a pair follows from its vector: R_ij = r_j - r_i
+    + n L with the unwrapped input positions, so n = round((R_ij - r_j +
+    r_i) L^-1) -- exact for FP32 vectors too (their error is ~1e-6 A against
+    lattice vectors of several A)."""
+    cap, cnt, jt, vec = plan.neighbors()
+    n = plan.natoms
+    dev = vec.device
+    sid = torch.repeat_interleave(torch.arange(len(nat), device=dev),
+                                  torch.as_tensor(nat, device=dev).long())
+    Linv = torch.linalg.inv(torch.as_tensor(cells, device=dev, dtype=torch.float64))[sid]
+    j = (jt & ((1 << 26) - 1)).long()
+    valid = torch.arange(cap, device=dev)[None, :] < cnt[:, None].long()
+    j = torch.where(valid, j, torch.zeros_like(j))
+    d = vec[..., :3].double() - (pos[j] - pos[:, None, :])
+    img = torch.einsum("ncx,nxy->ncy", d, Linv)
+    imgr = torch.round(img)
+    assert (img - imgr)[valid].abs().max().item() < 1e-3
+    code = (imgr.long() + 8)
+    assert ((code >= 0) & (code < 16))[valid].all()
+    key = j * 4096 + code[..., 0] * 256 + code[..., 1] * 16 + code[..., 2]
+    key = torch.where(valid, key, torch.full_like(key, 1 << 62))
+    return cnt.clone(), torch.sort(key, dim=1).values, vec.clone(), jt.clone()
+
+
 def test_fp32_and_fp64_plans_find_the_same_neighbours(cuda, oracle, tmp_path, nb_kernel):
-    """Both precisions decide the cut-off with the same FP64 predicate."""
+    """Both precisions decide the cut-off with the same FP64 predicate:
+    every row of the FP32 (mixed) plan's table holds the same set of
+    (neighbour, lattice image) pairs as the FP64 plan's, and the pair
+    vectors agree to FP32 rounding."""
     torch = cuda
     from aenet_gb300 import workloads
     from aenet_gb300.core import FP64, MIXED
@@ -377,16 +406,72 @@ def test_fp32_and_fp64_plans_find_the_same_neighbours(cuda, oracle, tmp_path, nb
         nat, pos, typ, cells, pbc = w.packed()
         p = torch.tensor(pos, device="cuda")
         t = torch.tensor(typ, device="cuda")
-        counts = []
+        got = []
         for prec in (FP64, MIXED):
             plan = Plan(nat, cells, pbc, precision=prec)
             plan.run(p, t)
             plan.check()
-            counts.append(plan.neighbors()[1].clone())
+            got.append(_neighbour_keys(torch, plan, p, cells, nat))
             plan.close()
-        assert torch.equal(counts[0], counts[1])
+        (c64, k64, v64, _), (c32, k32, v32, _) = got
+        assert torch.equal(c64, c32)
+        assert torch.equal(k64, k32)
+        assert int(c64.sum().item()) > 60 * len(pos)
+        # same pair vectors (matched through the sorted keys)
+        cap = k64.shape[1]
+        for v, c in ((v64, c64), (v32, c32)):
+            assert v.shape[1] == cap
+        d64 = torch.sort(v64[..., 3].double().masked_fill(
+            torch.arange(cap, device="cuda")[None] >= c64[:, None], 1e9), dim=1).values
+        d32 = torch.sort(v32[..., 3].double().masked_fill(
+            torch.arange(cap, device="cuda")[None] >= c32[:, None], 1e9), dim=1).values
+        assert (d64 - d32).abs().max().item() < 1e-5
     finally:
         ann.release()
+
+
+@pytest.mark.parametrize("acts", [((2, 3, 0), (3, 4, 0), (4, 2, 0)),
+                                  ((2, 2, 2), (3, 3, 3), (4, 4, 4))])
+def test_activation_codes_2_to_4(cuda, oracle, tmp_path, acts):
+    """ff_activate's sigmoid (2), scaled tanh 1.7159 tanh(2x/3) (3) and the
+    same plus 0.1x (4) (feedforward.f90:932-969) in hidden and output
+    layers: FP64 against the oracle to 1e-10 eV/atom, the mixed path on the
+    tensor-core kernel (its generic-activation instantiation) and on the
+    SIMT kernel within the mixed tolerance of FP64."""
+    from aenet_gb300 import nnfile, workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    w = workloads.lisio_batch_4096(nstruc=12)
+    rng = np.random.default_rng(21)
+    base = workloads.glorot_networks(rng, w.types, w.arch)
+    # activation codes of (hidden 1, hidden 2, output), one layout per species
+    for t, a in zip(w.types, acts):
+        base[t] = nnfile.make_network(w.arch, base[t]["W"], activations=list(a))
+    w.networks = base
+    paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    ann = _ann(paths, w.types)
+    try:
+        structs = [(s.positions, s.types, s.cell, True) for s in w.structures]
+        r64 = ann.batch_energy_forces(structs, precision=FP64)
+        out = {}
+        for mode in ("simt", "tensor"):
+            set_option("networks", mode)
+            out[mode] = ann.batch_energy_forces(structs, precision=MIXED)
+    finally:
+        set_option("networks", "tensor")
+        ann.release()
+    oracle.load(w.types, paths)
+    off = 0
+    for k, s in enumerate(w.structures):
+        _, et, F, _ = oracle.structure(s.cell, s.positions, s.types)
+        assert abs(r64["energy"][k] - et) / s.natoms < E_TOL_FP64, k
+        assert np.abs(r64["forces"][off:off + s.natoms] - F).max() < F_TOL_FP64, k
+        off += s.natoms
+    nat = np.array([s.natoms for s in w.structures])
+    for mode in ("simt", "tensor"):
+        dE = np.abs(out[mode]["energy"] - r64["energy"]) / nat
+        dF = out[mode]["forces"] - r64["forces"]
+        assert dE.max() < E_TOL_MIXED, (mode, dE.max())
+        assert np.sqrt((dF ** 2).mean()) < F_RMS_MIXED, mode
 
 
 def test_k3_cu_dimer_scan_on_gpu(cuda, tmp_path):
