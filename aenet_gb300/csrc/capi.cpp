@@ -414,7 +414,8 @@ void device_weights(const HostNet& net, NetTable& nt, std::vector<double>& w64) 
 // setup_symmfunc_Behler2011 (sfsetup.f90:1298) and stp_eval
 // (sfsetup.f90:925-944); the per-species table below is what
 // sf_fingerprint evaluates for a central atom of that species.
-int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out);
+int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out,
+                 int* grid_only);
 
 // Split-BF16 images of every species' network for the tensor-core kernel
 // (two hidden layers, input and hidden widths up to 64; TcLayout in
@@ -593,7 +594,7 @@ int build_device_tables() {
   std::vector<std::vector<unsigned char>> bt;
   std::vector<double> bt_rc;
   if (sftype == "behler2011") {
-    int st = build_behler(bt, bt_rc);
+    int st = build_behler(bt, bt_rc, &pd.behler_grid_only);
     if (st) return st;
   }
   size_t blob_bytes = 0;
@@ -681,9 +682,59 @@ BehlerFn make_fn(double Rc, double p1, double p2, double p3, int kind, int out) 
   return b;
 }
 
-int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out) {
+// Whether the angular functions fns[f0, f1) form a product grid (one kind,
+// one Rc, lambda = +-1, every (lambda, zeta) x eta combination once); fills
+// `gr` when they do.
+bool angular_grid(const std::vector<BehlerFn>& fns, int f0, int f1, BehlerGrid& gr) {
+  if (f1 - f0 < 2) return false;
+  memset(&gr, 0, sizeof(gr));
+  const BehlerFn& a = fns[f0];
+  if (a.kind != 4 && a.kind != 5) return false;
+  gr.kind = a.kind;
+  gr.Rc = a.Rc;
+  std::vector<std::pair<double, double>> lz;
+  std::vector<double> et;
+  for (int f = f0; f < f1; ++f) {
+    const BehlerFn& b = fns[f];
+    if (b.kind != a.kind || b.Rc != a.Rc || (b.p1 != 1.0 && b.p1 != -1.0) || !(b.p2 > 0.0))
+      return false;
+    auto key = std::make_pair(b.p1, b.p2);
+    if (std::find(lz.begin(), lz.end(), key) == lz.end()) lz.push_back(key);
+    if (std::find(et.begin(), et.end(), b.p3) == et.end()) et.push_back(b.p3);
+  }
+  if ((int)lz.size() > AE_BG_NL || (int)et.size() > AE_BG_NE) return false;
+  if ((int)(lz.size() * et.size()) != f1 - f0) return false;
+  gr.nl = (int)lz.size();
+  gr.ne = (int)et.size();
+  for (int q = 0; q < AE_BG_NL * AE_BG_NE; ++q) gr.out[q] = -1;
+  for (int f = f0; f < f1; ++f) {
+    const BehlerFn& b = fns[f];
+    int l = (int)(std::find(lz.begin(), lz.end(), std::make_pair(b.p1, b.p2)) - lz.begin());
+    int e = (int)(std::find(et.begin(), et.end(), b.p3) - et.begin());
+    if (gr.out[l * AE_BG_NE + e] >= 0) return false;
+    gr.out[l * AE_BG_NE + e] = b.out;
+  }
+  gr.fRc = (float)gr.Rc;
+  for (int l = 0; l < gr.nl; ++l) {
+    gr.lam[l] = lz[l].first;
+    gr.zeta[l] = lz[l].second;
+    gr.flam[l] = (float)gr.lam[l];
+    gr.fzeta[l] = (float)gr.zeta[l];
+    const double z = gr.zeta[l];
+    gr.izeta[l] = (z >= 1.0 && z <= 64.0 && z == std::floor(z)) ? (int)z : 0;
+  }
+  for (int e = 0; e < gr.ne; ++e) {
+    gr.eta[e] = et[e];
+    gr.feta[e] = (float)et[e];
+  }
+  return true;
+}
+
+int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<double>& rc_max_out,
+                 int* grid_only) {
   // sf_init over the global types (sfsetup.f90:800-808, symmfunc.f90:91-140)
   const int nt = g.ntypes;
+  *grid_only = 1;
   int nGmax = 0;
   for (auto& p : g.pots) nGmax = std::max(nGmax, p.stp.nsf);
   // registered functions: by (type1 global, pair/triple of LOCAL env
@@ -797,11 +848,28 @@ int build_behler(std::vector<std::vector<unsigned char>>& out, std::vector<doubl
     hdr.ang_off[nt * nt] = (int)fns.size();
     hdr.nfn = (int)fns.size();
     hdr.rc_max = rcm;
-    size_t bytes = sizeof(BehlerTable) + sizeof(BehlerFn) * (fns.size() + 1);
+    // product grids of the angular lists (evaluation order only; the
+    // functions and their feature indices are the ones listed above)
+    std::vector<BehlerGrid> grids;
+    for (int q = 0; q < nt * nt; ++q) {
+      hdr.grid_of[q] = -1;
+      BehlerGrid gr;
+      if (angular_grid(fns, hdr.ang_off[q], hdr.ang_off[q + 1], gr)) {
+        hdr.grid_of[q] = (int)grids.size();
+        grids.push_back(gr);
+      } else if (hdr.ang_off[q + 1] > hdr.ang_off[q]) {
+        *grid_only = 0;
+      }
+    }
+    size_t fbytes = sizeof(BehlerTable) + sizeof(BehlerFn) * (fns.size() + 1);
+    fbytes = (fbytes + 15) & ~size_t(15);
+    hdr.grid_off = grids.empty() ? 0 : (int)fbytes;
+    size_t bytes = fbytes + sizeof(BehlerGrid) * grids.size();
     std::vector<unsigned char> buf(bytes, 0);
     memcpy(buf.data(), &hdr, sizeof(BehlerTable));
     BehlerTable* bt = reinterpret_cast<BehlerTable*>(buf.data());
     if (!fns.empty()) memcpy(bt->fn, fns.data(), sizeof(BehlerFn) * fns.size());
+    if (!grids.empty()) memcpy(buf.data() + fbytes, grids.data(), sizeof(BehlerGrid) * grids.size());
     out.push_back(std::move(buf));
     rc_max_out.push_back(rcm);
   }

@@ -64,6 +64,25 @@ struct BehlerFn {     // one radial (G1..G3) or angular (G4, G5) function
   int pad;
 };
 
+// The angular functions of one neighbour-species pair when they form a
+// product grid: one kind (G4 or G5), one Rc, lambda = +-1, and every
+// combination of nl (lambda, zeta) pairs with ne eta values present once.
+// The kernels then evaluate per neighbour pair one exponential per eta and
+// one power per (lambda, zeta) instead of one of each per function.
+#define AE_BG_NL 16
+#define AE_BG_NE 8
+struct BehlerGrid {
+  int kind;                           // 4 or 5
+  int nl, ne;
+  int pad;
+  double Rc;
+  double lam[AE_BG_NL], zeta[AE_BG_NL], eta[AE_BG_NE];
+  float fRc;
+  float flam[AE_BG_NL], fzeta[AE_BG_NL], feta[AE_BG_NE];
+  int izeta[AE_BG_NL];                // zeta as an integer in [1, 64], else 0
+  int out[AE_BG_NL * AE_BG_NE];       // feature index of (l, e): out[l * AE_BG_NE + e]
+};
+
 // Per central species: functions grouped by neighbour species (radial) and
 // neighbour species pair (angular), with the feature index each feeds.
 struct BehlerTable {
@@ -71,6 +90,8 @@ struct BehlerTable {
   double rc_max;                      // largest Rc of any function
   int rad_off[AE_MAXT + 1];           // into fn[] by neighbour species
   int ang_off[AE_MAXT * AE_MAXT + 1]; // by (tj, tk) with tj <= tk
+  int grid_of[AE_MAXT * AE_MAXT];     // index of the pair's BehlerGrid, or -1
+  int grid_off;                       // byte offset of the BehlerGrid array
   int nfn;
   BehlerFn fn[1];                     // variable length (allocated larger)
 };
@@ -109,6 +130,7 @@ struct PotDevice {
   const double* w64;                  // weights, row-major W[o][k], pitch
   const float* w32;
   const unsigned char* behler_blob;   // BehlerTable per species
+  int behler_grid_only;               // every non-empty angular list is a BehlerGrid
   // tensor-core networks of the mixed path (two hidden layers): per species
   // an image of split-BF16 operand tiles and FP32 vectors (TcLayout)
   int tc_ok;                          // every species fits the tensor-core kernel
