@@ -238,61 +238,17 @@ __device__ __forceinline__ const BehlerGrid* grids_of(const BehlerTable* tab) {
                                              tab->grid_off);
 }
 
-// ---- pair schedules: lanes take pairs p = lane, lane + 32, ... of a list
+// ---- pair schedules: lanes take pairs p = lane, lane + 32, ... of a list.
 // Unordered pairs of one bucket of m neighbours on a circulant schedule:
 // p = q m + r -> (r, (r + q + 1) mod m); with q < (m - 1)/2, plus the pairs
 // at distance m/2 from r < m/2 when m is even, every pair occurs once.
-__device__ __forceinline__ void tri_pair(int p, int m, float inv_m, int& j, int& k) {
-  int q = __float2int_rz(((float)p + 0.5f) * inv_m);
-  int r = p - q * m;
-  if (r < 0) {
-    --q;
-    r += m;
-  } else if (r >= m) {
-    ++q;
-    r -= m;
-  }
-  j = r;
-  k = r + q + 1;
-  if (k >= m) k -= m;
-}
 // Pairs of bucket A (ma) x bucket C (mc): p = q ma + r -> (r, (q + r) mod mc).
-__device__ __forceinline__ void rect_pair(int p, int ma, float inv_ma, int mc, float inv_mc, int& j,
-                                          int& k) {
-  int q = __float2int_rz(((float)p + 0.5f) * inv_ma);
-  int r = p - q * ma;
-  if (r < 0) {
-    --q;
-    r += ma;
-  } else if (r >= ma) {
-    ++q;
-    r -= ma;
-  }
-  int kk = q + r;
-  kk -= mc * __float2int_rz(((float)kk + 0.5f) * inv_mc);
-  if (kk < 0)
-    kk += mc;
-  else if (kk >= mc)
-    kk -= mc;
-  j = r;
-  k = kk;
-}
-
+// Each lane keeps (q, r) and r mod mc and advances them by 32 with integer
+// adds and compares only (int <-> float conversions are slow on this GPU).
 struct PairList {
   int a0, ma, c0, mc, P;
-  float inv_a, inv_c;
+  int s32, mam;     // 32 mod mc, ma mod mc (rectangle)
   bool tri;
-  __device__ __forceinline__ void get(int p, int& j, int& k) const {
-    if (tri) {
-      tri_pair(p, ma, inv_a, j, k);
-      j += a0;
-      k += a0;
-    } else {
-      rect_pair(p, ma, inv_a, mc, inv_c, j, k);
-      j += a0;
-      k += c0;
-    }
-  }
 };
 
 __device__ __forceinline__ PairList pair_list(const int* bstart, int a, int c) {
@@ -303,10 +259,50 @@ __device__ __forceinline__ PairList pair_list(const int* bstart, int a, int c) {
   L.mc = bstart[c + 1] - bstart[c];
   L.tri = a == c;
   L.P = L.tri ? L.ma * (L.ma - 1) / 2 : L.ma * L.mc;
-  L.inv_a = 1.0f / (float)max(L.ma, 1);
-  L.inv_c = 1.0f / (float)max(L.mc, 1);
+  L.s32 = L.mc > 0 ? 32 % L.mc : 0;
+  L.mam = L.mc > 0 ? L.ma % L.mc : 0;
   return L;
 }
+
+struct PairWalk {
+  int p, q, r, rm;
+  __device__ __forceinline__ void init(const PairList& L, int lane) {
+    p = lane;
+    if (L.P == 0) return;
+    q = lane / L.ma;
+    r = lane - q * L.ma;
+    rm = L.tri ? 0 : r % L.mc;
+  }
+  __device__ __forceinline__ void get(const PairList& L, int& j, int& k) const {
+    if (L.tri) {
+      int kk = r + q + 1;
+      if (kk >= L.ma) kk -= L.ma;
+      j = L.a0 + r;
+      k = L.a0 + kk;
+    } else {
+      int kk = q + rm;
+      if (kk >= L.mc) kk -= L.mc;
+      j = L.a0 + r;
+      k = L.c0 + kk;
+    }
+  }
+  __device__ __forceinline__ void advance(const PairList& L) {
+    p += 32;
+    r += 32;
+    if (!L.tri) {
+      rm += L.s32;
+      if (rm >= L.mc) rm -= L.mc;
+    }
+    while (r >= L.ma) {
+      r -= L.ma;
+      ++q;
+      if (!L.tri) {
+        rm -= L.mam;
+        if (rm < 0) rm += L.mc;
+      }
+    }
+  }
+};
 
 // ---- powers of the grid path: F = u^zeta (and dF/du = zeta u^(zeta-1))
 __device__ __forceinline__ float ex2_approx(float x) {
@@ -392,22 +388,23 @@ template <typename T, typename Body>
 __device__ __forceinline__ void run_pairs(const PairList& L, const typename V4<T>::type* sR,
                                           bool filter, T Rc2, int* queue, int lane, Body body) {
   using T4 = typename V4<T>::type;
+  PairWalk w;
+  w.init(L, lane);
   if (!filter) {
-    for (int p = lane; p < L.P; p += 32) {
+    for (; w.p < L.P; w.advance(L)) {
       int j, k;
-      L.get(p, j, k);
+      w.get(L, j, k);
       body(j, k);
     }
     return;
   }
   const unsigned lt = (1u << lane) - 1u;
   int head = 0;
-  for (int p0 = 0; p0 < L.P; p0 += 32) {
-    const int p = p0 + lane;
+  for (int p0 = 0; p0 < L.P; p0 += 32, w.advance(L)) {
     int j = 0, k = 0;
     bool ok = false;
-    if (p < L.P) {
-      L.get(p, j, k);
+    if (w.p < L.P) {
+      w.get(L, j, k);
       const T4 Rj = sR[j], Rk = sR[k];
       const T dx = Rk.x - Rj.x, dy = Rk.y - Rj.y, dz = Rk.z - Rj.z;
       ok = dx * dx + dy * dy + dz * dz < Rc2;
@@ -485,7 +482,7 @@ __device__ void forward_grid(const BehlerGrid* gr, const PairList& L, const type
         const int ll = min(l0 + l, nl - 1);
         zeta[l] = gval<T>(gr, gr->zeta, gr->fzeta, ll);
         iz[l] = gr->izeta[ll];
-        pos[l] = gr->lam[ll] > 0.0;
+        pos[l] = gr->flam[ll] > 0.f;
       }
       T acc[BL][BE];
 #pragma unroll
@@ -540,9 +537,11 @@ __device__ void forward_generic(const BehlerTable* tab, int f0, int f1e, const P
     T acc[FCH];
 #pragma unroll
     for (int q = 0; q < FCH; ++q) acc[q] = T(0);
-    for (int p = lane; p < L.P; p += 32) {
+    PairWalk w;
+    w.init(L, lane);
+    for (; w.p < L.P; w.advance(L)) {
       int j, k;
-      L.get(p, j, k);
+      w.get(L, j, k);
       const T4 Rj = sR[j], Rk = sR[k];
       const T dxx = Rk.x - Rj.x, dyy = Rk.y - Rj.y, dzz = Rk.z - Rj.z;
       const T rjk2 = dxx * dxx + dyy * dyy + dzz * dzz;
@@ -704,7 +703,7 @@ __device__ void adjoint_grid(const BehlerGrid* gr, const PairList& L, const type
         const int ll = min(l0 + l, nl - 1);
         zeta[l] = gval<T>(gr, gr->zeta, gr->fzeta, ll);
         iz[l] = gr->izeta[ll];
-        pos[l] = gr->lam[ll] > 0.0;
+        pos[l] = gr->flam[ll] > 0.f;
 #pragma unroll
         for (int e = 0; e < BE; ++e)
           g[l][e] = (l0 + l < nl && e0 + e < ne) ? T(2) * sg[gr->out[(l0 + l) * AE_BG_NE + e0 + e]]
@@ -762,9 +761,11 @@ __device__ void adjoint_generic(const BehlerTable* tab, int f0, int f1e, const P
                                 const typename V4<T>::type* sR, const typename V4<T>::type* sA,
                                 const T* sg, T* sF, int lane) {
   using T4 = typename V4<T>::type;
-  for (int p = lane; p < L.P; p += 32) {
+  PairWalk w;
+  w.init(L, lane);
+  for (; w.p < L.P; w.advance(L)) {
     int j, k;
-    L.get(p, j, k);
+    w.get(L, j, k);
     const T4 Rj = sR[j], Rk = sR[k];
     const T invj = sA[j].x, invk = sA[k].x;
     const T dx = Rk.x - Rj.x, dy = Rk.y - Rj.y, dz = Rk.z - Rj.z;
