@@ -67,7 +67,9 @@ def _i32(a):
 
 
 def set_option(key, value):
-    """aenet_gpu_set_option (angular_domain, cell_div)."""
+    """aenet_gpu_set_option: angular_domain, angular_spin, angular_terms,
+    cell_div, z_refine, lanes_per_atom, adjoint_lanes_per_atom,
+    neighbour_kernel, networks (include/aenet_gb300.h)."""
     st = _lib.lib().aenet_gpu_set_option(key.encode(), str(value).encode())
     check_status(st)
 

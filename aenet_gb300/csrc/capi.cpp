@@ -274,6 +274,7 @@ struct State {
                              // per home atom (1), per home cell with a lane per candidate (2),
                              // warp per atom over the half stencil (3)
   int angular_moments = 1;   // FP32 angular terms in moment form where instantiated
+  int angular_spin_stale = 0;  // Chebyshev spin block with sfb_eval's stale s_j
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
@@ -916,6 +917,9 @@ struct aenet_gpu_plan {
   int* nb_img = nullptr;
   float* M = nullptr;         // angular moments of the FP32 moment form
   int mom_pad = 0;
+  int* nb_rank = nullptr;     // stale-spin order of the table slots (option angular_spin)
+  float* nb_seff = nullptr;
+  int stale_caller_order = 0; // table rows hold a caller's lists (rank = slot)
   void* G = nullptr;
   void* dEdG = nullptr;
   double* E_atom = nullptr;
@@ -1095,6 +1099,15 @@ int make_geom(StructGeom& G, const double* lat, int pbc, const double* coords, i
   return 0;
 }
 
+// the loaded potentials are Chebyshev bases with a spin block and the
+// stale-spin option is on
+bool stale_spin_wanted() {
+  if (!g.angular_spin_stale || !g.dev_ready) return false;
+  for (int t = 0; t < g.pd.ntypes; ++t)
+    if (g.pd.sp[t].sftype == AE_SF_CHEBYSHEV && g.pd.sp[t].cheb.multi) return true;
+  return false;
+}
+
 int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices) {
   const double rc = P->rc;
   int cell_off = 0, atom_off = 0, nchunks = 0;
@@ -1182,6 +1195,9 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
     if (aN <= AE_MOMA) P->mom_pad = (2 * aN * aN + 3) & ~3;
   }
   size_t o_M = P->mom_pad ? take(4 * (size_t)P->mom_pad * N) : 0;
+  const bool stale = stale_spin_wanted();
+  size_t o_rk = stale ? take(4 * npairs) : 0;
+  size_t o_se = stale ? take(4 * npairs) : 0;
   size_t o_G = take(tsz * nsf_pad * N);
   size_t o_dG = take(tsz * nsf_pad * N);
   size_t o_E = take(8 * (size_t)N);
@@ -1215,6 +1231,8 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->nb_vec = (void*)(b + o_vec);
   P->nb_img = P->keep_images ? (int*)(b + o_img) : nullptr;
   P->M = P->mom_pad ? (float*)(b + o_M) : nullptr;
+  P->nb_rank = stale ? (int*)(b + o_rk) : nullptr;
+  P->nb_seff = stale ? (float*)(b + o_se) : nullptr;
   P->G = (void*)(b + o_G);
   P->dEdG = (void*)(b + o_dG);
   P->E_atom = (double*)(b + o_E);
@@ -1297,6 +1315,11 @@ DescBuffers desc_buffers(aenet_gpu_plan* P, const double* grad_scale, bool viria
     d.M = P->M;
     d.mom_pad = P->mom_pad;
   }
+  if (P->nb_rank) {
+    d.nb_rank = P->nb_rank;
+    d.nb_seff = P->nb_seff;
+    d.M = nullptr;    // ordered spin weights need the pair form
+  }
   return d;
 }
 
@@ -1357,6 +1380,10 @@ int plan_networks(aenet_gpu_plan* P, const DescBuffers& d, cudaStream_t s) {
 int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s) {
   const PotDevice& pd = *P->pd;
   DescBuffers d = desc_buffers(P, nullptr, false);
+  if (d.nb_rank &&
+      ck(ae_launch_stale_order(P->natoms, P->geom_d, P->atom_struct, P->r_wrap, pd, d, P->fp64,
+                               P->stale_caller_order, P->nb_rank, P->nb_seff, s)))
+    return AENET_ERR_CUDA;
   int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
                                              : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
   if (ck(e)) return AENET_ERR_CUDA;
@@ -1526,9 +1553,53 @@ EXPORT double aenet_free_atom_energy(int type_id) {
 
 namespace {
 
+// Workspace of the per-atom calls: device scratch and a pinned staging
+// block that grow to the largest call seen and are then reused, and a
+// library stream.  A call copies its inputs in with one transfer and its
+// energy, status and forces out with one; nothing is allocated once the
+// buffers are large enough.  The buffers live until the process exits.
+struct AtomScratch {
+  char* dev = nullptr;
+  size_t dev_bytes = 0;
+  char* host = nullptr;
+  size_t host_bytes = 0;
+  cudaStream_t stream = nullptr;
+};
+AtomScratch g_atom;
+
+int atom_scratch_reserve(size_t dev_bytes, size_t host_bytes) {
+  if (!g_atom.stream && cudaStreamCreateWithFlags(&g_atom.stream, cudaStreamNonBlocking))
+    return AENET_ERR_CUDA;
+  if (g_atom.dev_bytes < dev_bytes) {
+    if (g_atom.dev) cudaFree(g_atom.dev);
+    g_atom.dev = nullptr;
+    g_atom.dev_bytes = 0;
+    const size_t want = std::max(dev_bytes, (size_t)1 << 20);
+    if (cudaMalloc((void**)&g_atom.dev, want) != cudaSuccess) {
+      g_atom.dev = nullptr;
+      return AENET_ERR_MALLOC;
+    }
+    g_atom.dev_bytes = want;
+  }
+  if (g_atom.host_bytes < host_bytes) {
+    if (g_atom.host) cudaFreeHost(g_atom.host);
+    g_atom.host = nullptr;
+    g_atom.host_bytes = 0;
+    const size_t want = std::max(host_bytes, (size_t)1 << 18);
+    if (cudaMallocHost((void**)&g_atom.host, want) != cudaSuccess) {
+      g_atom.host = nullptr;
+      return AENET_ERR_MALLOC;
+    }
+    g_atom.host_bytes = want;
+  }
+  return 0;
+}
+
 // One atom with caller-supplied neighbours, evaluated on the GPU as a
 // one-row neighbour table (aenet.f90:359-486).  F_local[(n_j+1)*3]
 // receives the forces on the central atom (row 0) and on each neighbour.
+// With the option angular_spin = stale the spin weights follow the
+// caller's neighbour order, as sfb_eval's do.
 int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, const int* type_j,
                 double* E_i, double* F_local) {
   if (!(g.init && g.loaded)) return AENET_ERR_INIT;
@@ -1540,9 +1611,29 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   const PotDevice& pd = g.pd;
   const int cap = std::max(32, (n_j + 31) & ~31);
   const bool fp64 = true;
+  const bool stale = stale_spin_wanted();
+  const size_t nsf_pad = pd.nsf_pad;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = (off + bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  // inputs (one upload), device-only work arrays, outputs (one download)
+  const size_t o_vec = take(32 * (size_t)cap), o_jt = take(4 * (size_t)cap), o_hdr = take(16);
+  const size_t up_bytes = off;
+  const size_t o_rk = stale ? take(4 * (size_t)cap) : 0, o_se = stale ? take(4 * (size_t)cap) : 0;
+  const size_t o_G = take(8 * nsf_pad), o_dG = take(8 * nsf_pad);
+  const size_t o_out = take(0);
+  const size_t out_bytes = 32 + 32 * (size_t)(n_j + 1);   // E, status, pad, force rows
+  take(out_bytes);
+  st = atom_scratch_reserve(off, std::max(up_bytes, out_bytes));
+  if (st) return st;
   // host neighbour row: R_ij = coo_j - coo_i (sfbasis.f90:488)
-  std::vector<double> vec(4 * (size_t)cap, 0.0);
-  std::vector<int> jt(cap, 0);
+  char* h = g_atom.host;
+  double* vec = (double*)(h + o_vec);
+  int* jt = (int*)(h + o_jt);
+  memset(h, 0, up_bytes);
   for (int j = 0; j < n_j; ++j) {
     double R[3];
     for (int c = 0; c < 3; ++c) R[c] = coo_j[3 * j + c] - coo_i[c];
@@ -1552,31 +1643,18 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
     vec[4 * j + 3] = std::sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
     jt[j] = (j + 1) | ((type_j[j] - 1) << AE_TYPE_SHIFT);
   }
-  const size_t nsf_pad = pd.nsf_pad;
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    size_t o = off;
-    off = (off + bytes + 255) & ~(size_t)255;
-    return o;
-  };
-  size_t o_vec = take(32 * (size_t)cap), o_jt = take(4 * (size_t)cap), o_cnt = take(4),
-         o_t = take(4), o_as = take(4), o_G = take(8 * nsf_pad), o_dG = take(8 * nsf_pad),
-         o_E = take(8), o_F = take(32 * (size_t)(n_j + 1)), o_st = take(16);
-  void* mem = nullptr;
-  if (cudaMalloc(&mem, off) != cudaSuccess) return AENET_ERR_MALLOC;
-  char* b = (char*)mem;
-  int zero = 0, t0 = type_i - 1, one = n_j;
-  cudaMemcpy(b + o_vec, vec.data(), 32 * (size_t)cap, cudaMemcpyHostToDevice);
-  cudaMemcpy(b + o_jt, jt.data(), 4 * (size_t)cap, cudaMemcpyHostToDevice);
-  cudaMemcpy(b + o_cnt, &one, 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(b + o_t, &t0, 4, cudaMemcpyHostToDevice);
-  cudaMemcpy(b + o_as, &zero, 4, cudaMemcpyHostToDevice);
-  cudaMemset(b + o_F, 0, 32 * (size_t)(n_j + 1));
-  cudaMemset(b + o_st, 0, 16);
+  int* hdr = (int*)(h + o_hdr);
+  hdr[0] = n_j;         // neighbour count
+  hdr[1] = type_i - 1;  // central species (0-based)
+  hdr[2] = 0;           // structure of the atom
+  char* b = g_atom.dev;
+  cudaStream_t s = g_atom.stream;
+  int e = (int)cudaMemcpyAsync(b, h, up_bytes, cudaMemcpyHostToDevice, s);
+  if (!e) e = (int)cudaMemsetAsync(b + o_out, 0, out_bytes, s);
   DescBuffers d{};
   d.natoms = 1;
-  d.types = (const int*)(b + o_t);
-  d.nb_cnt = (const int*)(b + o_cnt);
+  d.types = (const int*)(b + o_hdr + 4);
+  d.nb_cnt = (const int*)(b + o_hdr);
   d.nb_jt = (const int*)(b + o_jt);
   d.nb_vec = b + o_vec;
   d.cap = cap;
@@ -1584,28 +1662,37 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   d.lpa = 32;
   d.G = b + o_G;
   d.dEdG = b + o_dG;
-  d.E_atom = (double*)(b + o_E);
-  d.F = b + o_F;
+  d.E_atom = (double*)(b + o_out);
+  d.status = (unsigned*)(b + o_out + 8);
+  d.F = b + o_out + 32;
   d.virial = nullptr;
-  d.atom_struct = (const int*)(b + o_as);
+  d.atom_struct = (const int*)(b + o_hdr + 8);
   d.grad_scale = nullptr;
-  d.status = (unsigned*)(b + o_st);
-  cudaStream_t s = 0;
-  int e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, fp64, s)
-                                             : ae_launch_chebyshev_forward(pd, d, fp64, s);
+  const bool behler = pd.sp[0].sftype == AE_SF_BEHLER;
+  if (stale && !behler) {
+    d.nb_rank = (const int*)(b + o_rk);
+    d.nb_seff = (const float*)(b + o_se);
+    if (!e)
+      e = ae_launch_stale_order(1, nullptr, nullptr, nullptr, pd, d, 1, 1, (int*)(b + o_rk),
+                                (float*)(b + o_se), s);
+  }
+  if (!e) e = behler ? ae_launch_behler_forward(pd, d, fp64, s) : ae_launch_chebyshev_forward(pd, d, fp64, s);
   if (!e) e = ae_launch_mlp(pd, d, fp64, s);
   if (!e && F_local)
-    e = (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_adjoint(pd, d, fp64, s)
-                                           : ae_launch_chebyshev_adjoint(pd, d, fp64, s);
-  if (!e) e = (int)cudaMemcpy(E_i, b + o_E, 8, cudaMemcpyDeviceToHost);
-  if (!e && F_local) {
-    std::vector<double> f4(4 * (size_t)(n_j + 1));
-    e = (int)cudaMemcpy(f4.data(), b + o_F, f4.size() * 8, cudaMemcpyDeviceToHost);
+    e = behler ? ae_launch_behler_adjoint(pd, d, fp64, s) : ae_launch_chebyshev_adjoint(pd, d, fp64, s);
+  const size_t down = F_local ? out_bytes : 16;
+  if (!e) e = (int)cudaMemcpyAsync(h, b + o_out, down, cudaMemcpyDeviceToHost, s);
+  if (!e) e = (int)cudaStreamSynchronize(s);
+  if (e) return AENET_ERR_CUDA;
+  const unsigned status = *(const unsigned*)(h + 8);
+  if (status) return AENET_ERR_CUDA;
+  *E_i = *(const double*)h;
+  if (F_local) {
+    const double* f4 = (const double*)(h + 32);
     for (int q = 0; q <= n_j; ++q)
       for (int c = 0; c < 3; ++c) F_local[3 * q + c] = f4[4 * q + c];
   }
-  cudaFree(mem);
-  return e ? AENET_ERR_CUDA : 0;
+  return 0;
 }
 
 }  // namespace
@@ -1893,36 +1980,47 @@ EXPORT void aenet_nbl_init(double latt_vec[9], int natoms, int atom_types[], dou
     keep.cell_off = 0;
     keep.atom_off = 0;
     Pn->geom_h[0] = keep;
-    cudaMemcpy(Pn->geom_d, &keep, sizeof(StructGeom), cudaMemcpyHostToDevice);
+    if (cudaMemcpy(Pn->geom_d, &keep, sizeof(StructGeom), cudaMemcpyHostToDevice) != cudaSuccess)
+      return;
     P = Pn.release();
   }
   std::unique_ptr<aenet_gpu_plan> hold(P);
-  double* d_c = nullptr;
-  int* d_t = nullptr;
-  cudaMalloc(&d_c, 24 * (size_t)nat);
-  cudaMalloc(&d_t, 4 * (size_t)nat);
-  cudaMemcpy(d_c, coords, 24 * (size_t)nat, cudaMemcpyHostToDevice);
-  cudaMemcpy(d_t, atom_types, 4 * (size_t)nat, cudaMemcpyHostToDevice);
+  // coordinates and types on the device; every failure leaves the list
+  // uninitialised (aenet_nbl_neighbors then returns no neighbours)
+  struct DevFree {
+    void* p = nullptr;
+    ~DevFree() {
+      if (p) cudaFree(p);
+    }
+  } io;
+  if (cudaMalloc(&io.p, 28 * (size_t)nat) != cudaSuccess) {
+    io.p = nullptr;
+    return;
+  }
+  double* d_c = (double*)io.p;
+  int* d_t = (int*)(d_c + 3 * (size_t)nat);
+  if (cudaMemcpy(d_c, coords, 24 * (size_t)nat, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d_t, atom_types, 4 * (size_t)nat, cudaMemcpyHostToDevice) != cudaSuccess)
+    return;
   int ntmax = g.ntypes;
-  ae_launch_types(nat, d_t, P->types0, ntmax, P->status, 0);
+  if (ae_launch_types(nat, d_t, P->types0, ntmax, P->status, 0)) return;
   NbBuffers nb = nb_buffers(P);
-  ae_launch_neighbors(nat, d_c, P->types0, nb, 1, 0);
+  if (ae_launch_neighbors(nat, d_c, P->types0, nb, 1, 0)) return;
   g.nbl_cnt.resize(nat);
   g.nbl_jt.resize((size_t)nat * P->cap);
   g.nbl_img.resize((size_t)nat * P->cap);
   g.nbl_vec.resize((size_t)nat * P->cap * 4);
   g.nbl_s.resize(3 * (size_t)nat);
   g.nbl_cart.resize(3 * (size_t)nat);
-  cudaMemcpy(g.nbl_cnt.data(), P->nb_cnt, 4 * (size_t)nat, cudaMemcpyDeviceToHost);
-  cudaMemcpy(g.nbl_jt.data(), P->nb_jt, 4 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost);
-  cudaMemcpy(g.nbl_img.data(), P->nb_img, 4 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost);
-  cudaMemcpy(g.nbl_vec.data(), P->nb_vec, 32 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost);
-  cudaMemcpy(g.nbl_s.data(), P->s_wrap, 24 * (size_t)nat, cudaMemcpyDeviceToHost);
-  cudaMemcpy(g.nbl_cart.data(), P->r_wrap, 24 * (size_t)nat, cudaMemcpyDeviceToHost);
   unsigned status = 0;
-  cudaMemcpy(&status, P->status, 4, cudaMemcpyDeviceToHost);
-  cudaFree(d_c);
-  cudaFree(d_t);
+  if (cudaMemcpy(g.nbl_cnt.data(), P->nb_cnt, 4 * (size_t)nat, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(g.nbl_jt.data(), P->nb_jt, 4 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(g.nbl_img.data(), P->nb_img, 4 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(g.nbl_vec.data(), P->nb_vec, 32 * (size_t)nat * P->cap, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(g.nbl_s.data(), P->s_wrap, 24 * (size_t)nat, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(g.nbl_cart.data(), P->r_wrap, 24 * (size_t)nat, cudaMemcpyDeviceToHost) ||
+      cudaMemcpy(&status, P->status, 4, cudaMemcpyDeviceToHost))
+    return;
   if (cudaDeviceSynchronize() != cudaSuccess || status) return;
   g.nbl_natoms = nat;
   g.nbl_types.assign(atom_types, atom_types + nat);
@@ -2034,6 +2132,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
   if (k == "angular_terms") {
     if (v == "moments") g.angular_moments = 1;
     else if (v == "pairs") g.angular_moments = 0;
+    else return AENET_ERR_INPUT;
+    return AENET_OK;
+  }
+  if (k == "angular_spin") {
+    if (v == "stale") g.angular_spin_stale = 1;
+    else if (v == "own") g.angular_spin_stale = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;
   }
@@ -2159,6 +2263,8 @@ EXPORT int aenet_gpu_plan_loss_gradient(aenet_gpu_plan* P, const double* d_coord
   if (force_term && !d_F_target) return AENET_ERR_INPUT;
   // the force term needs the descriptor tangent, written for Chebyshev bases
   if (force_term && pd.sp[0].sftype != AE_SF_CHEBYSHEV) return AENET_ERR_INPUT;
+  // ... with each neighbour's own spin (angular_spin = own)
+  if (force_term && P->nb_rank) return AENET_ERR_INPUT;
   if (mode == AENET_GPU_LOSS_ENERGY)
     for (int t = 1; t < pd.ntypes; ++t)
       if (std::fabs(pd.sp[t].E_scale - pd.sp[0].E_scale) > 1e-12 * std::fabs(pd.sp[0].E_scale))
@@ -2461,12 +2567,14 @@ void nlist_release() { g_nlist.reset(); }
 int nlist_setup(NlistCtx& c, int nlocal, int nall, const double* x, size_t nnz, int cap, int cap_a,
                 int precision) {
   if (!c.stream && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking)) return AENET_ERR_CUDA;
-  if (!c.P || c.nlocal != nlocal || c.precision != precision || cap > c.cap || cap_a != c.cap_a) {
+  if (!c.P || c.nlocal != nlocal || c.precision != precision || cap > c.cap || cap_a != c.cap_a ||
+      (c.P->nb_rank != nullptr) != stale_spin_wanted()) {
     int st = 0;
     const int pbc = 0;
     c.P.reset(plan_new(1, &nlocal, nullptr, &pbc, x, precision, &g.pd, aenet_Rc_max, cap, false, &st));
     if (!c.P) return st ? st : AENET_ERR_CUDA;
     c.P->cap_a = std::min(cap_a, c.P->cap);
+    c.P->stale_caller_order = 1;   // the rows keep the engine's list order
     c.nlocal = nlocal;
     c.precision = precision;
     c.cap = c.P->cap;
@@ -2622,6 +2730,7 @@ EXPORT int aenet_gpu_plan_descriptor_jacobian(aenet_gpu_plan* P, int atom0, int 
                                               double* d_dG_i, double* d_dG_j, int* d_nbl,
                                               int* d_nnb, void* stream) {
   if (!P || !P->pd || !P->fp64 || !d_dG_i || !d_dG_j || !d_nbl || !d_nnb) return AENET_ERR_INPUT;
+  if (P->nb_rank) return AENET_ERR_INPUT;   // Jacobians with each neighbour's own spin only
   if (atom0 < 0 || count < 0 || atom0 + count > P->natoms) return AENET_ERR_INPUT;
   const PotDevice& pd = *P->pd;
   const int sft = pd.sp[0].sftype;
@@ -2758,6 +2867,9 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   e |= ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s);
   cudaEventRecord(ev[2], s);
   DescBuffers d = desc_buffers(P, nullptr, false);
+  if (d.nb_rank)
+    e |= ae_launch_stale_order(P->natoms, P->geom_d, P->atom_struct, P->r_wrap, pd, d, P->fp64,
+                               P->stale_caller_order, P->nb_rank, P->nb_seff, s);
   e |= (pd.sp[0].sftype == AE_SF_BEHLER) ? ae_launch_behler_forward(pd, d, P->fp64, s)
                                           : ae_launch_chebyshev_forward(pd, d, P->fp64, s);
   cudaEventRecord(ev[3], s);
@@ -2841,6 +2953,7 @@ namespace {
 bool cache_matches(const HostPlanCache& c, int nstruc, const int* natoms, const double* lattices,
                    const int* pbc, int precision) {
   if (!c.plan || c.precision != precision || (int)c.natoms.size() != nstruc || c.isolated) return false;
+  if ((c.plan->nb_rank != nullptr) != stale_spin_wanted()) return false;
   if (memcmp(c.natoms.data(), natoms, 4 * (size_t)nstruc)) return false;
   for (int s = 0; s < nstruc; ++s)
     if (c.pbc[s] != (pbc ? (pbc[s] ? 1 : 0) : 1)) return false;

@@ -263,7 +263,24 @@ struct DescBuffers {
   void* V;                     // [N][nsf_pad] (T) normalised descriptor tangents
   float* M;                    // [N][mom_pad] angular moments (FP32 moment form) or null
   int mom_pad;
+  // angular spin weights as sfb_eval forms them (sfbasis.f90:514, 556):
+  // the pair (j, k) of a row, j first in the reference's neighbour order,
+  // weighs s_eff(j) s(k), where s_eff(j) is the spin of the last neighbour
+  // up to j in that order inside the radial cut-off (1 before any).  Per
+  // table slot: the rank in that order and s_eff; null = s(j) s(k).
+  const int* nb_rank;          // [N*cap]
+  const float* nb_seff;        // [N*cap]
 };
+
+// rank and stale spin of every slot of the neighbour table in the
+// reference's lcl_nbdist_cart order (self images first, then atoms in
+// ascending index, each with its home copy first and then the images in
+// the order i3, i2, i1 with i1 fastest), or with caller_order in slot
+// order (rows built from a caller's list); Chebyshev bases only.  geom,
+// atom_struct and r_wrap are read only without caller_order.
+int ae_launch_stale_order(int natoms, const StructGeom* geom, const int* atom_struct,
+                          const double* r_wrap, const PotDevice& pd, const DescBuffers& b,
+                          int fp64, int caller_order, int* rank, float* seff, cudaStream_t s);
 
 int ae_launch_chebyshev_forward(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);

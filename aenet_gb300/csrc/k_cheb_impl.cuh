@@ -306,6 +306,20 @@ __device__ __forceinline__ void forward_moments(const PotDevice& pd, const DescB
   }
 }
 
+// Spin weight of the staged angular pair (a, k) with the reference's
+// stale s_j (sfbasis.f90:514, 556): the member first in the reference's
+// neighbour order contributes s_eff, the other its own spin.  f.z is the
+// neighbour's own spin, f.w its slot in the atom's table row.
+template <typename T>
+__device__ __forceinline__ T ordered_spin(const DescBuffers& b, int i,
+                                          const typename Vec4<T>::type& fa,
+                                          const typename Vec4<T>::type& fk) {
+  const size_t rb = (size_t)i * b.cap;
+  const int sa = (int)fa.w, sk = (int)fk.w;
+  return b.nb_rank[rb + sa] < b.nb_rank[rb + sk] ? T(b.nb_seff[rb + sa]) * fk.z
+                                                 : T(b.nb_seff[rb + sk]) * fa.z;
+}
+
 // ----------------------------------------------------------------------
 // forward
 // ----------------------------------------------------------------------
@@ -476,7 +490,10 @@ __global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_FWD_BLOCKS : 3) : 
           const T4 fk = sm.af[k];
           const T cosv = uj.x * uk.x + uj.y * uk.y + uj.z * uk.z;
           const T w = fj.x * fk.x;
-          const T sw = fj.z * fk.z * w;
+          T sw = fj.z * fk.z * w;
+          if constexpr (GUARD) {
+            if (b.nb_rank) sw = w * ordered_spin<T>(b, i, fj, fk);
+          }
           T x, dxdc;
           angular_arg(cosv, ct.angular_legacy, x, dxdc);
           const T x2 = x + x;
@@ -774,7 +791,10 @@ __global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_ADJ_BLOCKS : 3)
           const T4 fk = sm.af[k];
           const T cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
           const T w = fa.x * fk.x;
-          const T ss = fa.z * fk.z;
+          T ss = fa.z * fk.z;
+          if constexpr (GUARD) {
+            if (b.nb_rank) ss = ordered_spin<T>(b, i, fa, fk);
+          }
           T x, dxdc;
           angular_arg(cosv, ct.angular_legacy, x, dxdc);
           const T x2 = x + x;
@@ -908,14 +928,20 @@ int dispatch_moments(const PotDevice& pd, const DescBuffers& b, bool adjoint, cu
 // the moment form where it is instantiated.
 template <typename T>
 int dispatch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
+  int rN, aN;
+  const bool same = uniform_sizes(pd, rN, aN);
+  if (b.nb_rank) {
+    // ordered spin weights: pair form of the guarded instances
+    if (rN <= 24 && aN <= 16) return launch<T, 24, 16, 16, true, false>(pd, b, adjoint, s);
+    if (rN <= 32 && aN <= 32) return launch<T, 32, 32, 16, true, false>(pd, b, adjoint, s);
+    return (int)cudaErrorInvalidValue;
+  }
   if constexpr (sizeof(T) == 4) {
     if (b.M && pd.qleg) {
       const int e = dispatch_moments(pd, b, adjoint, s);
       if (e != AE_MOM_NA) return e;
     }
   }
-  int rN, aN;
-  const bool same = uniform_sizes(pd, rN, aN);
   if (same) {
     if (rN == 11 && aN == 5) return launch_lpa<T, 11, 5, false>(pd, b, adjoint, s);
     if (rN == 13 && aN == 7) return launch_lpa<T, 13, 7, false>(pd, b, adjoint, s);

@@ -64,6 +64,19 @@ extern "C" {
  *       sum rewritten by the addition theorem; cost linear in the angular
  *       neighbours, angular orders up to 6) or from the pair sum itself.
  *       Same values up to FP32 rounding; the FP64 path always sums pairs.
+ *   "angular_spin" = "own" | "stale"   spin weights of the Chebyshev
+ *       angular pairs (species-weighted bases).  own: s_j s_k.  stale: as
+ *       sfb_eval forms them (src/ext/sfbasis.f90:514, 556), where s_j is
+ *       refreshed only for neighbours inside the radial cut-off, so that
+ *       with a_Rc > r_Rc a neighbour beyond r_Rc carries the spin of the
+ *       last earlier neighbour inside it (1 before any).  The order is the
+ *       caller's for aenet_atomic_energy(_and_forces) and
+ *       aenet_gpu_neighbor_list_energy_forces, and for whole structures the
+ *       order of the reference's lcl_nbdist_cart (the atom's own images,
+ *       then the other atoms in ascending index, home copy before images).
+ *       Pair form only (the moment form is skipped); applies to plans
+ *       created afterwards; the force term of the training loss and the
+ *       descriptor Jacobians need "own" (AENET_ERR_INPUT otherwise).
  * Returns AENET_OK or AENET_ERR_INPUT.  "cell_div" and "z_refine" apply to
  * plans created afterwards, "angular_domain" from the next evaluation (the
  * device tables are rebuilt), the others from the next launch. */
@@ -286,11 +299,11 @@ int aenet_gpu_md_energy_fp64(aenet_gpu_md* md, double* E);
  * No counterpart in the reference (aenet runs on the CPU and allocates its
  * work arrays per call).  For callers that cannot allocate device memory
  * while they run -- MD engines that reserve all GPU memory at start-up and
- * forbid cudaMalloc in the time loop, hosts that capture their step in a
- * CUDA graph, plugins whose host owns the memory pool -- this computes the
- * energy and forces of ONE periodic structure using only the caller's
- * device buffers plus a fixed scratch array compiled into the library
- * (about 19.3 MiB per GPU, held until the process exits).
+ * forbid cudaMalloc in the time loop, plugins whose host application owns
+ * the memory pool -- this computes the energy and forces of ONE periodic
+ * structure using only the caller's device buffers plus a fixed scratch
+ * array compiled into the library (about 19.3 MiB per GPU, held until the
+ * process exits).
  *
  * Inputs (device): d_coords[3*natoms] Cartesian, d_types[natoms] 1-based;
  * lattice[9] (HOST) rows = lattice vectors.  Outputs (device, any may be
@@ -307,7 +320,16 @@ int aenet_gpu_md_energy_fp64(aenet_gpu_md* md, double* E);
  * The first call on each device looks up the scratch address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the one scratch array: calls that overlap on the GPU
- * (different streams, threads) race and give wrong results. */
+ * (different streams, threads) race and give wrong results.  The call
+ * reads the loaded potentials' device tables: do not load, reload or
+ * release potentials while calls are queued or running.
+ * Kernels: the one-warp-per-atom neighbour search on the unrefined grid,
+ * the pair form of the angular terms and the SIMT networks (the options
+ * neighbour_kernel, z_refine, angular_terms, angular_spin and networks do
+ * not apply; mixed results differ from aenet_gpu_structure_energy_forces
+ * by FP32 rounding).  Angular neighbours are staged up to a count sized
+ * from the structure's density (at most AENET_NOALLOC_MAX_NEIGHBORS);
+ * more set AENET_GPU_ST_NB_OVERFLOW. */
 #define AENET_NOALLOC_MAX_ATOMS 2048
 #define AENET_NOALLOC_MAX_NEIGHBORS 192
 #define AENET_NOALLOC_MAX_CELLS 65536

@@ -766,3 +766,91 @@ def test_host_batch_runs_in_chunks_like_one_plan(cuda, oracle, tmp_path):
             assert np.abs(V - one["virial"][None]).max() < 1e3 * tol * max(1, np.abs(one["virial"]).max())
     finally:
         ann.release()
+
+
+def test_stale_spin_option_matches_oracle(cuda, oracle, tmp_path):
+    """sfb_eval refreshes s_j only inside the radial branch (sfbasis.f90:514)
+    and reuses it for the angular pairs (:556): with a_Rc > r_Rc a neighbour
+    beyond r_Rc weighs its pairs with the spin of the last earlier neighbour
+    inside r_Rc.  Option angular_spin = stale reproduces that: the
+    structure path in the reference's lcl_nbdist_cart order (the oracle's
+    complete candidate order) and the per-atom libaenet calls in the
+    caller's order (also shuffled).  FP64 to 1e-10 eV/atom and 1e-9 eV/A;
+    with each neighbour's own spin the same potential differs from the
+    oracle; the mixed path stays within its tolerance."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    rng = np.random.default_rng(41)
+    w = workloads.aucu_fcc_4000()
+    s0 = w.structures[0]
+    sites, _ = workloads.fcc_positions(10, 3.90)
+    keep = np.all(sites < 3 * 3.90 - 0.1, axis=1)
+    s = workloads.Structure(s0.positions[keep], s0.types[keep], np.eye(3) * (3 * 3.90))
+    arch = [28, 16, 16, 1]
+    w = workloads.Workload("aucu_stale", w.types, workloads.cheb_setups(w.types, 8, 4.0, 4, 5.2),
+                           arch, [s], 2)
+    w.networks = workloads.glorot_networks(rng, w.types, arch)
+    paths = helpers.make_potentials(oracle, w, str(tmp_path))
+    oracle.load(w.types, paths)
+    ec, et, F_or, Ea_or = oracle.structure(s.cell, s.positions, s.types)
+    _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types)
+    ann = _ann(paths, w.types)
+    n = s.natoms
+    try:
+        set_option("angular_spin", "stale")
+        r64 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64)
+        r32 = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=MIXED)
+        assert abs(r64["energy"] - et) / n < E_TOL_FP64
+        assert np.abs(r64["atomic_energies"] - Ea_or).max() < E_TOL_FP64
+        assert np.abs(r64["forces"] - F_or).max() < F_TOL_FP64
+        assert abs(r32["energy"] - r64["energy"]) / n < E_TOL_MIXED
+        assert np.sqrt(np.mean((r32["forces"] - r64["forces"]) ** 2)) < F_RMS_MIXED
+        # per-atom calls: the caller's order decides, as in libaenet
+        for i in (0, 37, 101):
+            nbcoo, _, nbl, nbt = nb[i]
+            for perm in (np.arange(len(nbl)), rng.permutation(len(nbl))):
+                sym = [w.types[t - 1] for t in nbt[perm]]
+                Fg = np.zeros((n, 3))
+                Fo = np.zeros((n, 3))
+                eg = ann.atomic_energy_and_forces(centres[i], w.types[s.types[i] - 1], i + 1,
+                                                  nbcoo[perm], sym, nbl[perm], Fg)
+                eo = oracle.atomic_energy_and_forces(centres[i], int(s.types[i]), i + 1,
+                                                     nbcoo[perm], nbt[perm], nbl[perm], Fo)
+                assert abs(eg - eo) < E_TOL_FP64, (i, eg, eo)
+                assert np.abs(Fg - Fo).max() < F_TOL_FP64
+        set_option("angular_spin", "own")
+        own = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=FP64)
+    finally:
+        set_option("angular_spin", "own")
+        ann.release()
+    # the option matters for this basis: own spins miss the reference
+    assert np.abs(own["atomic_energies"] - Ea_or).max() > 1e-6
+
+
+def test_per_atom_calls_reuse_their_buffers(cuda, oracle, cu256):
+    """Repeated aenet_atomic_energy_and_forces calls (the predict.x calling
+    pattern) give identical results call after call and across neighbour
+    counts that grow and shrink (the staging buffers are grown once and
+    reused)."""
+    w, paths = cu256
+    s = w.structures[0]
+    oracle.load(w.types, paths)
+    _, centres, nb = oracle.neighbors(s.cell, s.positions, s.types)
+    ann = _ann(paths, w.types)
+    try:
+        first = {}
+        for rep in range(3):
+            for i in (5, 0, 200):
+                nbcoo, _, nbl, nbt = nb[i]
+                m = len(nbl) if rep != 1 else len(nbl) // 2
+                F = np.zeros((s.natoms, 3))
+                e = ann.atomic_energy_and_forces(centres[i], "Cu", i + 1, nbcoo[:m],
+                                                 ["Cu"] * m, nbl[:m], F)
+                key = (i, m)
+                if key in first:
+                    assert e == first[key][0]
+                    assert np.array_equal(F, first[key][1])
+                else:
+                    first[key] = (e, F)
+    finally:
+        ann.release()
