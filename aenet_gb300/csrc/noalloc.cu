@@ -4,17 +4,28 @@
 // Who needs this: codes that must not call cudaMalloc once they run --
 // molecular-dynamics engines that set up all device memory at start-up and
 // forbid allocation inside the time loop (allocation can synchronise the
-// device or fail after fragmentation), hosts that capture their step in a
-// CUDA graph (no allocation may happen while a stream is being captured),
-// and plugin environments whose host application owns the device memory
-// pool.  They pass device buffers for the inputs and outputs; everything
-// else the pass needs lives in one file-scope __device__ array of fixed
-// size that every GPU loading this library holds until the process exits.
+// device or fail after fragmentation), and plugin environments whose host
+// application owns the device memory pool.  They pass device buffers for
+// the inputs and outputs; everything else the pass needs lives in one
+// file-scope __device__ array of fixed size that every GPU loading this
+// library holds until the process exits.
 //
 // Limits: AENET_NOALLOC_MAX_ATOMS atoms, AENET_NOALLOC_MAX_NEIGHBORS
 // neighbours per atom, AENET_NOALLOC_MAX_CELLS cells of the neighbour
 // grid; larger inputs are rejected with AENET_ERR_MALLOC before anything
 // is launched.
+//
+// Kernels: the neighbour search with one warp per atom on the unrefined
+// grid, the pair form of the angular terms, the SIMT networks; the options
+// neighbour_kernel, z_refine, angular_terms, angular_spin and networks do
+// not apply (each neighbour carries its own spin), so mixed-precision
+// results differ from aenet_gpu_structure_energy_forces by FP32 rounding
+// only.  The staged angular neighbours per atom follow the structure's
+// density (as the plans do, at most the neighbour limit) and the lanes per
+// atom of the descriptor kernels are raised when their shared memory would
+// not fit.
+#include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "../../include/aenet_gb300.h"
@@ -151,8 +162,31 @@ extern "C" __attribute__((visibility("default"))) int aenet_gpu_structure_energy
   d.nb_jt = nb.nb_jt;
   d.nb_vec = nb.nb_vec;
   d.cap = (int)NA_NB;
-  d.cap_a = (int)NA_NB;
+  // staged angular neighbours: the expected count inside the largest
+  // angular cut-off with half again as many and 16 spare (as the plans size
+  // them), at most the neighbour limit
+  {
+    const double* a = lattice;
+    const double c0 = a[4] * a[8] - a[5] * a[7], c1 = a[5] * a[6] - a[3] * a[8],
+                 c2 = a[3] * a[7] - a[4] * a[6];
+    const double vol = std::fabs(a[0] * c0 + a[1] * c1 + a[2] * c2);
+    double arc = 0.0;
+    for (int t = 0; t < pd.ntypes; ++t)
+      arc = std::max(arc, pd.sp[t].sftype == AE_SF_CHEBYSHEV ? pd.sp[t].cheb.a_Rc : rc);
+    const double ra = arc + 1e-3;
+    const double nexp = vol > 0 ? 4.18879020478639 * ra * ra * ra * natoms / vol : (double)NA_NB;
+    int ca = (int)std::ceil(1.5 * nexp + 16.0);
+    ca = (ca + 7) & ~7;
+    d.cap_a = std::min(std::max(ca, 8), (int)NA_NB);
+  }
+  // lanes per atom: as set, raised while the descriptor kernels' shared
+  // memory per block (4 warps of 32 / lpa atoms) would exceed 200 KB
   d.lpa = ae_lanes_per_atom();
+  {
+    const size_t t4 = fp64 ? 32 : 16;
+    const size_t group = (2 * t4 + 3 * tsz) * (size_t)d.cap_a + tsz * (size_t)pd.nsf_pad + 32;
+    while (d.lpa < 32 && group * (size_t)(4 * 32 / d.lpa) > 200 * 1024) d.lpa *= 2;
+  }
   d.G = b + O_G;
   d.dEdG = b + O_DG;
   d.E_atom = (double*)(b + O_EA);

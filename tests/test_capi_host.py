@@ -135,3 +135,17 @@ def test_no_cpu_fallback_without_gpu(lib, tmp_path):
         assert st.value == 5
     finally:
         _final(lib)
+
+
+def test_noalloc_entry_point_requires_loaded_tables():
+    """Without loaded potentials the allocation-free entry point returns
+    AENET_ERR_INIT before it touches the GPU or any of its pointers."""
+    import ctypes as C
+    import numpy as np
+    from aenet_gb300 import _lib
+    lib = _lib.lib()
+    lat = np.ascontiguousarray(np.eye(3) * 10.0)
+    fake = C.c_void_p(256)     # never dereferenced: the call returns first
+    rc = lib.aenet_gpu_structure_energy_forces_noalloc(
+        4, fake, fake, lat.ctypes.data_as(C.c_void_p), 0, None, None, None, None, None)
+    assert rc == 1

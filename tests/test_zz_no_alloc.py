@@ -2,9 +2,9 @@
 
 aenet_gpu_structure_energy_forces_noalloc serves callers that cannot
 allocate device memory while they run (MD engines that reserve all GPU
-memory up front, CUDA-graph capture, plugin hosts owning the memory pool):
-it takes device buffers and keeps its scratch in an array compiled into the
-library.  Here it is called through the C-ABI twice in a row -- the second
+memory up front and forbid allocation in their time loop, plugin hosts
+whose application owns the memory pool): it takes device buffers and keeps
+its scratch in an array compiled into the library.  Here it is called through the C-ABI twice in a row -- the second
 call sees the first call's leftovers in the shared scratch -- and each
 result must match aenet_gpu_structure_energy_forces on the same structure
 within the tolerances the other GPU tests use.  The file runs last so that a
@@ -50,7 +50,7 @@ def setup(oracle, tmp_path_factory):
     ann.release()
 
 
-def _noalloc(torch, lib, s, precision):
+def _noalloc(torch, lib, s, precision, status=0):
     n = s.natoms
     d_pos = torch.tensor(s.positions, device="cuda")
     d_typ = torch.tensor(s.types, device="cuda", dtype=torch.int32)
@@ -67,8 +67,20 @@ def _noalloc(torch, lib, s, precision):
         stream)
     assert rc == 0, rc
     torch.cuda.synchronize()
-    assert int(d_st.item()) == 0
+    assert int(d_st.item()) == status, int(d_st.item())
     return d_E.item(), d_F.cpu().numpy(), d_W.cpu().numpy().reshape(3, 3)
+
+
+def _compare(ref, got, n, prec, FP64):
+    E, F, W = got
+    if prec == FP64:
+        assert abs(E - ref["energy"]) / n < E_TOL_FP64, (E, ref["energy"])
+        assert np.abs(F - ref["forces"]).max() < F_TOL_FP64
+        assert np.abs(W - ref["virial"]).max() < 1e-8
+    else:
+        assert abs(E - ref["energy"]) / n < E_TOL_MIXED
+        assert np.sqrt(np.mean((F - ref["forces"]) ** 2)) < F_RMS_MIXED
+        assert np.abs(W - ref["virial"]).max() < 1e-2 * max(1.0, np.abs(ref["virial"]).max())
 
 
 def test_noalloc_matches_allocating_entry_point(setup):
@@ -82,15 +94,41 @@ def test_noalloc_matches_allocating_entry_point(setup):
         ref = ann.structure_energy_forces(s.positions, s.types, s.cell, precision=prec,
                                           virial=True)
         for call in range(2):
-            E, F, W = _noalloc(torch, lib, s, prec)
-            if prec == FP64:
-                assert abs(E - ref["energy"]) / n < E_TOL_FP64, (call, E, ref["energy"])
-                assert np.abs(F - ref["forces"]).max() < F_TOL_FP64
-                assert np.abs(W - ref["virial"]).max() < 1e-8
-            else:
-                assert abs(E - ref["energy"]) / n < E_TOL_MIXED
-                assert np.sqrt(np.mean((F - ref["forces"]) ** 2)) < F_RMS_MIXED
-                assert np.abs(W - ref["virial"]).max() < 1e-2 * max(1.0, np.abs(ref["virial"]).max())
+            _compare(ref, _noalloc(torch, lib, s, prec), n, prec, FP64)
+
+
+def test_noalloc_eight_lanes_and_triclinic_cell(setup):
+    """Eight lanes per atom (the descriptor kernels' smallest groups, whose
+    FP64 adjoint needs the most shared memory) and a sheared cell, both
+    precisions, two calls each, against the allocating entry point."""
+    torch, ann, s = setup
+    from aenet_gb300 import _lib, workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    lib = _lib.lib()
+    shear = np.array([[1.0, 0.0, 0.0], [0.18, 1.0, 0.0], [-0.11, 0.07, 1.0]])
+    tric = workloads.Structure(s.positions @ shear, s.types, s.cell @ shear)
+    try:
+        set_option("lanes_per_atom", 8)
+        for st in (s, tric):
+            for prec in (FP64, MIXED):
+                ref = ann.structure_energy_forces(st.positions, st.types, st.cell, precision=prec,
+                                                  virial=True)
+                for call in range(2):
+                    _compare(ref, _noalloc(torch, lib, st, prec), st.natoms, prec, FP64)
+    finally:
+        set_option("lanes_per_atom", 16)
+
+
+def test_noalloc_reports_neighbour_overflow(setup):
+    """A cell compressed until its atoms have more neighbours than the
+    fixed per-atom limit (192): the call returns, and the status word it
+    writes carries the neighbour-overflow bit."""
+    torch, ann, s = setup
+    from aenet_gb300 import _lib, workloads
+    from aenet_gb300.core import FP64
+    lib = _lib.lib()
+    dense = workloads.Structure(s.positions * 0.62, s.types, s.cell * 0.62)
+    _noalloc(torch, lib, dense, FP64, status=1)     # AENET_GPU_ST_NB_OVERFLOW
 
 
 def test_noalloc_rejects_oversized_input(setup):
