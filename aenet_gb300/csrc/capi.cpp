@@ -1557,19 +1557,31 @@ namespace {
 // block that grow to the largest call seen and are then reused, and a
 // library stream.  A call copies its inputs in with one transfer and its
 // energy, status and forces out with one; nothing is allocated once the
-// buffers are large enough.  The buffers live until the process exits.
+// buffers are large enough.  The sequence of one call (copy in, kernels,
+// copy out) is captured once per row capacity as a CUDA graph and then
+// replayed, one launch per call.  The buffers live until the process exits.
+struct AtomGraph {
+  int cap, forces, stale, gen;
+  cudaGraphExec_t exec;
+};
 struct AtomScratch {
   char* dev = nullptr;
   size_t dev_bytes = 0;
   char* host = nullptr;
   size_t host_bytes = 0;
   cudaStream_t stream = nullptr;
+  std::vector<AtomGraph> graphs;
+  void drop_graphs() {
+    for (auto& q : graphs) cudaGraphExecDestroy(q.exec);
+    graphs.clear();
+  }
 };
 AtomScratch g_atom;
 
 int atom_scratch_reserve(size_t dev_bytes, size_t host_bytes) {
   if (!g_atom.stream && cudaStreamCreateWithFlags(&g_atom.stream, cudaStreamNonBlocking))
     return AENET_ERR_CUDA;
+  if (g_atom.dev_bytes < dev_bytes || g_atom.host_bytes < host_bytes) g_atom.drop_graphs();
   if (g_atom.dev_bytes < dev_bytes) {
     if (g_atom.dev) cudaFree(g_atom.dev);
     g_atom.dev = nullptr;
@@ -1625,7 +1637,7 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   const size_t o_rk = stale ? take(4 * (size_t)cap) : 0, o_se = stale ? take(4 * (size_t)cap) : 0;
   const size_t o_G = take(8 * nsf_pad), o_dG = take(8 * nsf_pad);
   const size_t o_out = take(0);
-  const size_t out_bytes = 32 + 32 * (size_t)(n_j + 1);   // E, status, pad, force rows
+  const size_t out_bytes = 32 + 32 * (size_t)(cap + 1);   // E, status, pad, force rows
   take(out_bytes);
   st = atom_scratch_reserve(off, std::max(up_bytes, out_bytes));
   if (st) return st;
@@ -1649,8 +1661,6 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   hdr[2] = 0;           // structure of the atom
   char* b = g_atom.dev;
   cudaStream_t s = g_atom.stream;
-  int e = (int)cudaMemcpyAsync(b, h, up_bytes, cudaMemcpyHostToDevice, s);
-  if (!e) e = (int)cudaMemsetAsync(b + o_out, 0, out_bytes, s);
   DescBuffers d{};
   d.natoms = 1;
   d.types = (const int*)(b + o_hdr + 4);
@@ -1669,19 +1679,53 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   d.atom_struct = (const int*)(b + o_hdr + 8);
   d.grad_scale = nullptr;
   const bool behler = pd.sp[0].sftype == AE_SF_BEHLER;
-  if (stale && !behler) {
+  const bool use_stale = stale && !behler;
+  if (use_stale) {
     d.nb_rank = (const int*)(b + o_rk);
     d.nb_seff = (const float*)(b + o_se);
-    if (!e)
+  }
+  const size_t down = F_local ? out_bytes : 16;
+  // the whole call on the stream: copy in, clear outputs, kernels, copy out
+  auto enqueue = [&]() -> int {
+    int e = (int)cudaMemcpyAsync(b, h, up_bytes, cudaMemcpyHostToDevice, s);
+    if (!e) e = (int)cudaMemsetAsync(b + o_out, 0, out_bytes, s);
+    if (!e && use_stale)
       e = ae_launch_stale_order(1, nullptr, nullptr, nullptr, pd, d, 1, 1, (int*)(b + o_rk),
                                 (float*)(b + o_se), s);
+    if (!e) e = behler ? ae_launch_behler_forward(pd, d, fp64, s) : ae_launch_chebyshev_forward(pd, d, fp64, s);
+    if (!e) e = ae_launch_mlp(pd, d, fp64, s);
+    if (!e && F_local)
+      e = behler ? ae_launch_behler_adjoint(pd, d, fp64, s) : ae_launch_chebyshev_adjoint(pd, d, fp64, s);
+    if (!e) e = (int)cudaMemcpyAsync(h, b + o_out, down, cudaMemcpyDeviceToHost, s);
+    return e;
+  };
+  const int fkey = F_local ? 1 : 0, skey = use_stale ? 1 : 0;
+  cudaGraphExec_t exec = nullptr;
+  for (auto& q : g_atom.graphs)
+    if (q.cap == cap && q.forces == fkey && q.stale == skey && q.gen == g.gen) exec = q.exec;
+  if (!exec) {
+    // capture this call's sequence once for the row capacity
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int e = enqueue();
+      const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+      if (!e && ee == cudaSuccess && graph &&
+          cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+        std::vector<AtomGraph> keep;
+        for (auto& q : g_atom.graphs) {
+          if (q.gen == g.gen) keep.push_back(q);
+          else cudaGraphExecDestroy(q.exec);
+        }
+        g_atom.graphs.swap(keep);
+        g_atom.graphs.push_back(AtomGraph{cap, fkey, skey, g.gen, exec});
+      } else {
+        exec = nullptr;
+      }
+      if (graph) cudaGraphDestroy(graph);
+    }
+    cudaGetLastError();   // a failed capture leaves nothing behind: run directly
   }
-  if (!e) e = behler ? ae_launch_behler_forward(pd, d, fp64, s) : ae_launch_chebyshev_forward(pd, d, fp64, s);
-  if (!e) e = ae_launch_mlp(pd, d, fp64, s);
-  if (!e && F_local)
-    e = behler ? ae_launch_behler_adjoint(pd, d, fp64, s) : ae_launch_chebyshev_adjoint(pd, d, fp64, s);
-  const size_t down = F_local ? out_bytes : 16;
-  if (!e) e = (int)cudaMemcpyAsync(h, b + o_out, down, cudaMemcpyDeviceToHost, s);
+  int e = exec ? (int)cudaGraphLaunch(exec, s) : enqueue();
   if (!e) e = (int)cudaStreamSynchronize(s);
   if (e) return AENET_ERR_CUDA;
   const unsigned status = *(const unsigned*)(h + 8);
@@ -2317,9 +2361,32 @@ struct aenet_gpu_md {
   int *types = nullptr, *flag = nullptr;
   long long steps = 0;
   int builds = 0;
+  // device time of the force part of each step (table build or refresh,
+  // descriptors, networks, adjoint), by kind of step; events of the last
+  // step are read at the next synchronisation
+  double ms_build = 0.0, ms_refresh = 0.0;
+  long long n_build = 0, n_refresh = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int pending = -1;           // -1 none, 0 refresh step, 1 build step
   ~aenet_gpu_md() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
     if (mem) cudaFree(mem);
     if (stream) cudaStreamDestroy(stream);
+  }
+  void collect() {
+    if (pending < 0) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) {
+      if (pending) {
+        ms_build += ms;
+        ++n_build;
+      } else {
+        ms_refresh += ms;
+        ++n_refresh;
+      }
+    }
+    pending = -1;
   }
 };
 
@@ -2470,6 +2537,9 @@ EXPORT int aenet_gpu_md_run(aenet_gpu_md* M, int nsteps, double* E_pot, double* 
         return AENET_ERR_CUDA;
       rebuild = h != 0;
     }
+    M->collect();   // the previous step's events are complete after the sync
+    if (!M->ev0 && (cudaEventCreate(&M->ev0) || cudaEventCreate(&M->ev1))) return AENET_ERR_CUDA;
+    if (cudaEventRecord(M->ev0, s)) return AENET_ERR_CUDA;
     int st;
     if (rebuild) {
       st = md_build(M);
@@ -2485,6 +2555,8 @@ EXPORT int aenet_gpu_md_run(aenet_gpu_md* M, int nsteps, double* E_pot, double* 
       if (!st) st = plan_adjoint(P, nullptr, M->F, 1.0, nullptr, s);
     }
     if (st) return st;
+    if (cudaEventRecord(M->ev1, s)) return AENET_ERR_CUDA;
+    M->pending = rebuild ? 1 : 0;
     if (ck(ae_md_kick(M->n, M->vel, M->F, M->invm, half_dt_acc, s))) return AENET_ERR_CUDA;
     ++M->steps;
   }
@@ -2494,6 +2566,7 @@ EXPORT int aenet_gpu_md_run(aenet_gpu_md* M, int nsteps, double* E_pot, double* 
   double h[2];
   if (cudaMemcpyAsync(h, M->scal, 16, cudaMemcpyDeviceToHost, s) || cudaStreamSynchronize(s))
     return AENET_ERR_CUDA;
+  M->collect();
   if (E_pot) *E_pot = h[0];
   if (E_kin) *E_kin = h[1];
   return AENET_OK;
@@ -2508,6 +2581,16 @@ EXPORT int aenet_gpu_md_get(aenet_gpu_md* M, double* coords, double* velocities,
       (forces && cudaMemcpyAsync(forces, M->F, b, cudaMemcpyDeviceToHost, s)) ||
       cudaStreamSynchronize(s))
     return AENET_ERR_CUDA;
+  return AENET_OK;
+}
+
+EXPORT int aenet_gpu_md_phase_times(aenet_gpu_md* M, double* build_ms, long long* build_steps,
+                                    double* refresh_ms, long long* refresh_steps) {
+  if (!M) return AENET_ERR_INPUT;
+  if (build_ms) *build_ms = M->ms_build;
+  if (build_steps) *build_steps = M->n_build;
+  if (refresh_ms) *refresh_ms = M->ms_refresh;
+  if (refresh_steps) *refresh_steps = M->n_refresh;
   return AENET_OK;
 }
 
@@ -2857,13 +2940,14 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   if (!P || !ms) return AENET_ERR_INPUT;
   cudaStream_t s = (cudaStream_t)stream;
   const PotDevice& pd = *P->pd;
-  cudaEvent_t ev[8];
-  for (int q = 0; q < 8; ++q) cudaEventCreate(&ev[q]);
+  cudaEvent_t ev[9];
+  for (int q = 0; q < 9; ++q) cudaEventCreate(&ev[q]);
   int e = 0;
   cudaEventRecord(ev[0], s);
   e |= ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s);
   cudaEventRecord(ev[1], s);
   NbBuffers nb = nb_buffers(P);
+  nb.ev_search = ev[8];
   e |= ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s);
   cudaEventRecord(ev[2], s);
   DescBuffers d = desc_buffers(P, nullptr, false);
@@ -2889,7 +2973,8 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   cudaEventRecord(ev[7], s);
   if (cudaEventSynchronize(ev[7]) != cudaSuccess) e = 1;
   for (int q = 0; q < 7; ++q) cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]);
-  for (int q = 0; q < 8; ++q) cudaEventDestroy(ev[q]);
+  cudaEventElapsedTime(&ms[7], ev[8], ev[2]);
+  for (int q = 0; q < 9; ++q) cudaEventDestroy(ev[q]);
   return e ? AENET_ERR_CUDA : 0;
 }
 

@@ -229,6 +229,7 @@ struct NbBuffers {
   void* nb_vec;               // float4 or double4_32a
   int* nb_img;                // optional: image T packed 3 x 10-bit signed
   unsigned* status;
+  cudaEvent_t ev_search;      // optional: recorded right before the search kernel
   int cell_kernel;            // 0: warp per atom; warp per home cell with a lane per
                               // home atom (1) or a lane per candidate (2); 3: warp per
                               // atom over the half stencil, each pair written to both rows

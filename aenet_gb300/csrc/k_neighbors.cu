@@ -1198,6 +1198,7 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
   k_scan_sums<<<1, SCAN_B, 0, s>>>(nblk, nb.scan_tmp, nb.cell_start + nc);
   k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
   k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
+  if (nb.ev_search) cudaEventRecord(nb.ev_search, s);
   if (nb.cell_kernel == 3) {
     e = cudaMemsetAsync(nb.nb_cnt, 0, sizeof(int) * (size_t)natoms, s);
     if (e != cudaSuccess) return (int)e;

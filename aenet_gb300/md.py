@@ -85,6 +85,15 @@ class MolecularDynamics:
                                                  f.ctypes.data_as(C.c_void_p)))
         return r, v, f
 
+    def phase_times(self):
+        """Device time of the force part of the steps so far: (ms of steps
+        that rebuilt the neighbour table, their count, ms of steps that
+        refreshed the stored pair vectors, their count)."""
+        bm, bs, rm, rs = C.c_double(), C.c_longlong(), C.c_double(), C.c_longlong()
+        check_status(_lib.lib().aenet_gpu_md_phase_times(self._h, C.byref(bm), C.byref(bs),
+                                                         C.byref(rm), C.byref(rs)))
+        return bm.value, bs.value, rm.value, rs.value
+
     def counters(self):
         steps, builds = C.c_longlong(), C.c_int()
         check_status(_lib.lib().aenet_gpu_md_counters(self._h, C.byref(steps), C.byref(builds)))

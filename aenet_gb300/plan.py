@@ -180,12 +180,12 @@ class Plan:
         return loss, grad
 
     STAGES = ("types", "neighbours", "descriptor", "networks", "energy_reduce", "adjoint",
-              "forces_out")
+              "forces_out", "neighbour_search")
 
     def profile(self, pos, types, E=None, F=None):
         """Stage durations (ms) of one full pass, CUDA events on the stream."""
         self._check_inputs(pos, types)
-        ms = (C.c_float * 7)()
+        ms = (C.c_float * 8)()
         check_status(_lib.lib().aenet_gpu_plan_profile(self._h, _p(pos), _p(types), _p(E), _p(F),
                                                        ms, _stream()))
         self.generation += 1

@@ -162,7 +162,7 @@ def neighbour_stats(plan, a_rc, r_rc):
     na = ((d <= a_rc) & (d >= 1e-12) & valid).sum(1).double()
     P = na * (na - 1) / 2
     return {"n_r": nr.mean().item(), "n_a": na.mean().item(), "P": P.mean().item(),
-            "cap": cap, "n_max": int(cnt.max().item())}
+            "n_all": cnt.double().mean().item(), "cap": cap, "n_max": int(cnt.max().item())}
 
 
 def cheb_flops(nb, R, A, nsf, m, arch):
@@ -370,52 +370,56 @@ def run_gb300(args):
     _lib.lib().aenet_gpu_measure_fp32_peak(C.byref(peak), C.c_void_p(stream.cuda_stream))
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0}
-    kernels = {"descriptor": "k_cheb_forward", "adjoint": "k_cheb_adjoint",
-               "networks": "k_mlp_tc", "neighbours": "k_neighbors"}
-    dom = max(kernels, key=lambda k: stages.get(k, 0.0))
-    cap = nb["cap"]
-    # algorithmic bytes per atom of each kernel (neighbour table at 20 B per
-    # pair: float4 vector + packed index; descriptor rows 4 B per feature;
-    # moment rows written by the forward and read by the adjoint)
+    # Per-kernel rooflines.  k_neighbors: HBM bound, the algorithmic bytes
+    # B_nl = 3 w + 4 + 16 + 8 n per atom (FP64 positions read, type, cell
+    # id / key / value, a neighbour index written and read back per pair),
+    # over the search kernel's own CUDA-event time.  Descriptor and adjoint:
+    # the FP32 pipe with the pair-form flop counts per atom (the moment form
+    # does fewer flops, so these are effective rates).  Networks: tensor
+    # pipe, reported as FP32-equivalent rates of the same flop counts.
     nsf = sp["nsf"]
-    # moment rows of the FP32 moment form (both blocks, padded to float4)
-    mom = 4 * ((2 * A * A + 3) & ~3) if (args.angular_terms == "moments" and A <= 7) else 0
-    nbytes = {"descriptor": nb["n_r"] * 20 + nsf * 4 + mom,
-              "adjoint": nb["n_r"] * 20 + nsf * 4 + 16 * (nb["n_r"] + 1) + mom,
-              "networks": 2 * nsf * 4 + 8,
-              "neighbours": 24 + nb["n_r"] * 20 + 16 * 27}
-    dom_ms = stages[dom]
-    traffic = None
+    hbm = peaks.get("hbm_gbs")
+    b_nl = 3 * 8 + 4 + 16 + 8 * nb["n_all"]
+    traffic_per_atom = {}
     tf = os.path.join(ROOT, "profiles", "traffic_per_atom.txt")
     if os.path.exists(tf):
-        per_atom = json.load(open(tf)).get(kernels[dom])
-        traffic = None if per_atom is None else per_atom * N
-    # what limits the kernel, from the ncu capture of the same kernels
-    limiter = None
+        traffic_per_atom = json.load(open(tf))
+    limiters = {}
     lf = os.path.join(ROOT, "profiles", "limiters_lisio_batch_512.txt")
     if os.path.exists(lf):
-        lim = json.load(open(lf)).get(kernels[dom])
-        if lim:
-            limiter = dict(lim, source="profiles/ncu_full_lisio_batch_512.md (ncu --set full)")
-    if dom in ("descriptor", "adjoint", "networks"):
-        ach = fl[dom] * N / (dom_ms * 1e-3) / 1e12
-        roof = {"bound": "fp32", "kernel": kernels[dom], "achieved": ach, "peak": peak.value,
-                "unit": "TFLOP/s", "frac": ach / peak.value if peak.value else None,
-                "traffic": traffic,
-                "peak_source": "measured live: FP32 FMA throughput kernel on this GPU",
-                "flops_per_atom": fl[dom], "ms_per_launch": dom_ms,
-                "hbm": {"achieved": nbytes[dom] * N / (dom_ms * 1e-3) / 1e9,
-                        "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                        "frac": nbytes[dom] * N / (dom_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs"),
-                        "bytes_per_atom": nbytes[dom]}}
-    else:
-        ach = nbytes[dom] * N / (dom_ms * 1e-3) / 1e9
-        roof = {"bound": "hbm", "kernel": kernels[dom], "achieved": ach,
-                "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                "frac": ach / peaks.get("hbm_gbs"), "traffic": traffic,
-                "bytes_per_atom": nbytes[dom], "ms_per_launch": dom_ms}
-    if limiter:
-        roof["limiter"] = limiter
+        limiters = json.load(open(lf))
+    times = {"k_neighbors": stages["neighbour_search"], "k_cheb_forward": stages["descriptor"],
+             "k_cheb_adjoint": stages["adjoint"], "k_mlp_tc": stages["networks"]}
+    kernels_roof = {}
+    for k, ms_k in times.items():
+        if k == "k_neighbors":
+            ach = b_nl * N / (ms_k * 1e-3) / 1e9
+            r = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                 "frac": ach / hbm, "bytes_per_atom": b_nl,
+                 "bytes_formula": "3*8 + 4 + 16 + 8*n_all per atom (n_all = %.2f)" % nb["n_all"]}
+            alg = b_nl * N
+        else:
+            f = {"k_cheb_forward": fl["descriptor"], "k_cheb_adjoint": fl["adjoint"],
+                 "k_mlp_tc": fl["networks"]}[k]
+            ach = f * N / (ms_k * 1e-3) / 1e12
+            r = {"bound": "fp32" if k != "k_mlp_tc" else "tensor", "achieved": ach,
+                 "peak": peak.value, "unit": "TFLOP/s",
+                 "frac": ach / peak.value if peak.value else None, "flops_per_atom": f,
+                 "peak_source": "measured live: FP32 FMA throughput kernel on this GPU"}
+            alg = None
+        r["ms_per_launch"] = ms_k
+        tpa = traffic_per_atom.get(k)
+        r["traffic"] = None if tpa is None else tpa * N
+        if tpa is not None and alg:
+            r["traffic_over_algorithmic"] = tpa * N / alg
+        if limiters.get(k):
+            r["limiter"] = dict(limiters[k], source="profiles/ncu_full_lisio_batch_512.md")
+        kernels_roof[k] = r
+    dom = max(times, key=lambda k: times[k])
+    roof = dict(kernels_roof[dom], kernel=dom)
+    roof["other_kernels"] = {k: {q: v for q, v in r.items() if q in ("bound", "achieved", "frac",
+                                                                     "unit", "ms_per_launch")}
+                             for k, r in kernels_roof.items() if k != dom}
     plan32.close()
 
     # ---- plain FP64 path on the same batch
@@ -475,6 +479,45 @@ def run_gb300(args):
         # same kernels, neighbour order within a cell may differ: FP32 noise
         dev_e = np.abs(hE.numpy() - res32["E"].cpu().numpy()) / nat
         assert dev_e.max() < 1e-5, dev_e.max()
+        # cold calls: every call brings a batch layout the previous call did
+        # not have (the structures alternately in their order and reversed),
+        # so the cached plans are rebuilt and their graphs captured anew
+        offs = np.concatenate([[0], np.cumsum(nat)])
+        rev = np.arange(S)[::-1]
+        layouts = []
+        for order in (np.arange(S), rev):
+            idx = np.concatenate([np.arange(offs[k], offs[k + 1]) for k in order])
+            hp_o = torch.empty((N, 3), dtype=torch.float64, pin_memory=True)
+            hp_o.copy_(torch.from_numpy(np.ascontiguousarray(pos[idx])))
+            ht_o = torch.empty(N, dtype=torch.int32, pin_memory=True)
+            ht_o.copy_(torch.from_numpy(np.ascontiguousarray(typ[idx])))
+            layouts.append((np.ascontiguousarray(nat[order], dtype=np.int32), hp_o, ht_o,
+                            np.ascontiguousarray(cells[order].reshape(S, 9)),
+                            np.ascontiguousarray(pbc[order], dtype=np.int32)))
+
+        def call_layout(L):
+            n_o, hp_o, ht_o, c_o, p_o = L
+            lib.aenet_gpu_batch_energy_forces(
+                S, n_o.ctypes.data_as(C.c_void_p), C.c_void_p(hp_o.data_ptr()),
+                C.c_void_p(ht_o.data_ptr()), c_o.ctypes.data_as(C.c_void_p),
+                p_o.ctypes.data_as(C.c_void_p), MIXED, C.c_void_p(hE.data_ptr()),
+                C.c_void_p(hF.data_ptr()), None, C.byref(st))
+            if st.value:
+                raise RuntimeError("aenet_gpu_batch_energy_forces status %d" % st.value)
+
+        cold = []
+        ncold = max(3, args.steps // 4)
+        for k in range(ncold + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call_layout(layouts[(k + 1) % 2])
+            if k:   # the first alternation only leaves the warm layout
+                cold.append(time.perf_counter() - t0)
+        cold_s = float(np.mean(cold))
+        e2e["cold"] = {"value": job_rate(N, cold_s, device=dev), "unit": "atoms/s",
+                       "ms_per_step": 1e3 * cold_s, "calls": len(cold),
+                       "note": "each call a new batch layout (structure order alternated): "
+                               "plans and graphs rebuilt inside the timed call"}
 
     # ---- CPU baseline (rank 0): the oracle port on a bounded sample
     cpu = None
@@ -493,12 +536,30 @@ def run_gb300(args):
         o.close()
 
     # ---- training step on the same batch: loss E + F and its weight gradient
+    # against targets of an FP64 teacher potential of the same shape (random
+    # networks from seed 104, the batch's descriptor normalisation)
     train = None
     if not args.no_train:
+        from aenet_gb300 import nnfile
         from aenet_gb300.plan import LOSS_ENERGY_FORCES
+        stats = {}
+        for tname in w.types:
+            _, stp_t, _, _ = nnfile.read_nn(paths[tname])
+            stats[tname] = (stp_t["sfval_min"], stp_t["sfval_max"], stp_t["sfval_avg"],
+                            stp_t["sfval_cov"])
+        teacher_nets = workloads.glorot_networks(np.random.default_rng(104), w.types, w.arch)
+        tpaths = workloads.write_potentials(w, tempfile.mkdtemp(prefix="aenet_teacher_"),
+                                            stats=stats, networks=teacher_nets)
+        ann.release()
+        tann = ANNPotentials(tpaths)
+        plan_e = Plan(nat, cells, pbc, precision=FP64, coords0=pos)
+        tout = plan_e.run(p, t)
+        plan_e.check()
+        E_t, F_t = tout["E"].clone(), tout["F"].clone()
+        plan_e.close()
+        tann.release()
+        ann = ANNPotentials(paths)
         plan_t = Plan(nat, cells, pbc, precision=MIXED, coords0=pos)
-        E_t = (res32["E"] + 0.01 * natoms_t).contiguous()
-        F_t = (0.9 * res32["F"]).contiguous()
         gbuf = torch.empty(ann.nweights(), dtype=torch.float64, device=dev)
         lbuf = torch.empty(1, dtype=torch.float64, device=dev)
 
@@ -509,20 +570,34 @@ def run_gb300(args):
         for _ in range(max(1, args.warmup)):
             tstep()
         plan_t.check()
+        tgraph = None
+        if not args.no_graph:
+            tgraph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(tgraph):
+                tstep()
+            tgraph.replay()
+            torch.cuda.synchronize()
         tms = []
         for _ in range(max(3, args.steps // 4)):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            tstep()
+            if tgraph is not None:
+                tgraph.replay()
+            else:
+                tstep()
             b.record(stream)
             b.synchronize()
             tms.append(a.elapsed_time(b))
+        plan_t.check()
         tm = float(np.mean(tms))
-        train = {"workload": "same batch: loss w_E sum (E-E_t)^2/N^2 + w_F sum |F-F_t|^2 and "
-                             "its gradient with respect to all %d weights" % ann.nweights(),
+        train = {"workload": "same batch: loss w_E sum (E-E_t)^2/N^2 + w_F sum |F-F_t|^2, "
+                             "w_E 1, w_F 0.1, targets from an FP64 teacher potential of the same "
+                             "shape (seed 104), gradient with respect to all %d weights"
+                             % ann.nweights(),
                  "atoms_per_s": N / (tm * 1e-3), "ms_per_step": tm, "precision": "mixed",
-                 "loss": float(lbuf.item())}
+                 "cuda_graph": tgraph is not None, "loss": float(lbuf.item())}
+        del tgraph
         plan_t.close()
 
     ann.release()
@@ -603,6 +678,61 @@ def time_cpu(o, s, threads, seconds):
     return k / dt, k
 
 
+def per_atom_leg(w, paths, s):
+    """The predict.x calling pattern through the libaenet C-ABI: one
+    aenet_atomic_energy_and_forces call per atom with its neighbour list
+    (lcl_nbdist_cart order), host arrays in and out, against the same calls
+    of the oracle port on one host thread."""
+    from aenet_gb300 import _lib
+    from oracle import Oracle
+    lib = _lib.lib()
+    o = Oracle()
+    o.load(w.types, paths)
+    _, centres, nb = o.neighbors(s.cell, s.positions, s.types)
+    n = s.natoms
+    rows = []
+    for i in range(n):
+        nbcoo, _, nbl, nbt = nb[i]
+        rows.append((np.ascontiguousarray(centres[i]), int(s.types[i]), i + 1, len(nbl),
+                     np.ascontiguousarray(nbcoo), np.ascontiguousarray(nbt, dtype=np.int32),
+                     np.ascontiguousarray(nbl, dtype=np.int32)))
+    F = np.zeros((n, 3))
+    E = C.c_double()
+    st = C.c_int()
+
+    def gpu_pass_rows():
+        F[:] = 0.0
+        etot = 0.0
+        for ci, ti, ii, m, co, ty, ix in rows:
+            lib.aenet_atomic_energy_and_forces(
+                ci.ctypes.data_as(C.c_void_p), ti, ii, m, co.ctypes.data_as(C.c_void_p),
+                ty.ctypes.data_as(C.c_void_p), ix.ctypes.data_as(C.c_void_p), n, C.byref(E),
+                F.ctypes.data_as(C.c_void_p), C.byref(st))
+            if st.value:
+                raise RuntimeError("aenet_atomic_energy_and_forces status %d" % st.value)
+            etot += E.value
+        return etot
+
+    gpu_pass_rows()
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        e_gpu = gpu_pass_rows()
+    dt_gpu = (time.perf_counter() - t0) / reps
+    Fo = np.zeros((n, 3))
+    t0 = time.perf_counter()
+    e_cpu = 0.0
+    for ci, ti, ii, m, co, ty, ix in rows:
+        e_cpu += o.atomic_energy_and_forces(ci, ti, ii, co, ty, ix, Fo)
+    dt_cpu = time.perf_counter() - t0
+    o.close()
+    return {"api": "aenet_atomic_energy_and_forces (one call per atom, host arrays)",
+            "us_per_call": 1e6 * dt_gpu / n, "atoms_per_s": n / dt_gpu,
+            "cpu_1_thread_us_per_call": 1e6 * dt_cpu / n, "cpu_1_thread_atoms_per_s": n / dt_cpu,
+            "speedup_vs_cpu_1_thread": dt_cpu / dt_gpu,
+            "energy_diff_eV": abs(e_gpu - e_cpu), "force_max_diff_eV_per_A": float(np.abs(F - Fo).max())}
+
+
 def run_configs(args, local, flush, fp32_peak):
     """Energy and forces of the single-structure configurations, FP64 and
     mixed, device-timed (CUDA graph replays, L2 flushed between steps), the
@@ -667,6 +797,8 @@ def run_configs(args, local, flush, fp32_peak):
                                          "flops_adj_per_atom": adj}
                 del graph
                 plan.close()
+            if name == "cu_fcc_256":
+                row["per_atom_api"] = per_atom_leg(w, paths, s)
             dE = abs(res["mixed"]["E"] - res["fp64"]["E"]).item() / s.natoms
             dF = res["mixed"]["F"] - res["fp64"]["F"]
             row["mixed_over_fp64"] = row["mixed"]["atoms_per_s"] / row["fp64"]["atoms_per_s"]
@@ -737,12 +869,22 @@ def run_md(args, local):
             drift.append(abs(ep + ek - e0) / s.natoms)
         steps, builds = md.counters()
         nsteps = steps - steps0
+        bm, bn, rm, rn = md.phase_times()
+        _, _, Fmd = md.state()
+        force_rms = float(np.sqrt(np.mean(Fmd ** 2)))
         out = {"workload": "cuau_fcc_1m: 64^3 conventional FCC cells, a = 3.70 A, 25% Au, "
                            "sigma 0.1 A, Chebyshev r16/6.0 a8/4.0 (52 features), 52-20-20-1 x2",
                "atoms": s.natoms, "steps": int(nsteps), "dt_fs": 2.0, "skin_A": 0.3,
                "precision": "mixed forces, fp64 integration",
                "atom_steps_per_s": s.natoms * nsteps / run_s, "ms_per_step": 1e3 * run_s / nsteps,
                "neighbour_builds": int(builds - builds0),
+               "force_part_ms_per_step": {
+                   "with_table_build": bm / bn if bn else None, "build_steps": int(bn),
+                   "with_refresh": rm / rn if rn else None, "refresh_steps": int(rn),
+                   "note": "device time of neighbour table (build or pair refresh), "
+                           "descriptors, networks and forces; the rest of a step is the "
+                           "integration kernels and the per-step skin check"},
+               "force_rms_eV_per_A": force_rms,
                "fp64_monitor_max_eV_per_atom": max(monitor),
                "energy_drift_max_eV_per_atom": max(drift),
                "timing": "host wall clock around md.run blocks of 10 steps (one sync per "

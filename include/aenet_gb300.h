@@ -144,9 +144,10 @@ int aenet_gpu_plan_backward(aenet_gpu_plan* plan, const double* d_weights,
                             double* d_grad, double* d_virial, void* stream);
 
 /* The full pass with forces, with CUDA events recorded on `stream` between
- * the stages; ms[7] receives the stage durations in milliseconds: type
- * check, neighbour search, descriptor, networks, energy reduction,
- * adjoint, force output.  Synchronises the stream. */
+ * the stages; ms[8] receives the stage durations in milliseconds: type
+ * check, neighbour search (cell lists and search), descriptor, networks,
+ * energy reduction, adjoint, force output, and last the search kernel
+ * alone (part of the second entry).  Synchronises the stream. */
 int aenet_gpu_plan_profile(aenet_gpu_plan* plan, const double* d_coords,
                            const int* d_types, double* d_E, double* d_F,
                            float* ms, void* stream);
@@ -290,6 +291,11 @@ int aenet_gpu_md_run(aenet_gpu_md* md, int nsteps, double* E_pot, double* E_kin)
 /* host copies of the current state (any may be NULL) */
 int aenet_gpu_md_get(aenet_gpu_md* md, double* coords, double* velocities,
                      double* forces);
+/* device time (ms) of the force part of the steps so far, split into
+ * steps that rebuilt the neighbour table and steps that refreshed the
+ * stored pair vectors (each includes descriptors, networks and forces) */
+int aenet_gpu_md_phase_times(aenet_gpu_md* md, double* build_ms, long long* build_steps,
+                             double* refresh_ms, long long* refresh_steps);
 /* steps taken and neighbour-table builds so far */
 int aenet_gpu_md_counters(aenet_gpu_md* md, long long* steps, int* builds);
 /* plain FP64 energy of the current positions (the mixed run's monitor) */
