@@ -529,10 +529,13 @@ def run_gb300(args):
         threads = os.cpu_count() or 1
         sample = pick_sample(o, w.structures, threads, args.cpu_seconds)
         n, dt = time_oracle(o, sample, threads)
+        s1 = pick_sample(o, w.structures, 1, args.cpu_seconds / 5)
+        n1, dt1 = time_oracle(o, s1, 1)
         cpu = {"value": n / dt, "unit": "atoms/s", "cores": threads, "kind": "port",
                "sample": "first %d of %d cells (%d atoms), FP64 oracle port of predict.x "
                          "(linked-cell search as written), %d OpenMP threads, %.1f s"
-                         % (len(sample), S, n, threads, dt)}
+                         % (len(sample), S, n, threads, dt),
+               "one_thread": {"value": n1 / dt1, "sample_atoms": n1, "seconds": dt1}}
         o.close()
 
     # ---- training step on the same batch: loss E + F and its weight gradient

@@ -13,7 +13,8 @@ computed here -- and stores them as small ``.npz`` files:
                      total energies (F20.8) and the forces (F12.6) printed in
                      output-reference/dimer-x*.xsf.out.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
+        (or with the environment variable AENET_REFERENCE_ROOT set)
 """
 import glob
 import os
@@ -81,4 +82,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AENET_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set AENET_REFERENCE_ROOT)")
+    main(root)
