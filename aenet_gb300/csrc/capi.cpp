@@ -920,6 +920,8 @@ struct aenet_gpu_plan {
   int* nb_rank = nullptr;     // stale-spin order of the table slots (option angular_spin)
   float* nb_seff = nullptr;
   int stale_caller_order = 0; // table rows hold a caller's lists (rank = slot)
+  int* struct_order = nullptr;  // structures by decreasing size (per-structure search)
+  int smem_atoms = 0, smem_cells = 0;
   void* G = nullptr;
   void* dEdG = nullptr;
   double* E_atom = nullptr;
@@ -1210,6 +1212,15 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_ord = take(4 * (size_t)N);
   size_t o_spo = take(4 * (AE_MAXT + 1));
   size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(N));
+  // per-structure search: every structure's cell lists fit one block's
+  // shared memory (at most 48 KB with the unit tables)
+  int max_n = 0, max_c = 0;
+  for (int s = 0; s < P->nstruc; ++s) {
+    max_n = std::max(max_n, P->natoms_h[s]);
+    max_c = std::max(max_c, P->geom_h[s].nc[0] * P->geom_h[s].nc[1] * P->geom_h[s].nc[2]);
+  }
+  const bool per_struct = 20 * (size_t)max_n + 4 * ((size_t)max_c + 1) + 24576 <= 48 * 1024;
+  size_t o_so2 = per_struct ? take(4 * (size_t)P->nstruc) : 0;
   if (cudaMalloc(&P->mem, off) != cudaSuccess) return AENET_ERR_CUDA;
   P->mem_bytes = off;
   char* b = (char*)P->mem;
@@ -1245,6 +1256,16 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->order = (int*)(b + o_ord);
   P->spec_off = (int*)(b + o_spo);
   P->part_scratch = (int*)(b + o_ps);
+  P->struct_order = per_struct ? (int*)(b + o_so2) : nullptr;
+  P->smem_atoms = max_n;
+  P->smem_cells = max_c;
+  if (per_struct) {
+    std::vector<int> ord(P->nstruc);
+    for (int s = 0; s < P->nstruc; ++s) ord[s] = s;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int c) { return P->natoms_h[a] > P->natoms_h[c]; });
+    cudaMemcpy(P->struct_order, ord.data(), 4 * (size_t)P->nstruc, cudaMemcpyHostToDevice);
+  }
   std::vector<int> as(N);
   for (int s = 0, a = 0; s < P->nstruc; ++s)
     for (int q = 0; q < P->natoms_h[s]; ++q) as[a++] = s;
@@ -1346,6 +1367,9 @@ NbBuffers nb_buffers(aenet_gpu_plan* P) {
   nb.nb_img = P->nb_img;
   nb.status = P->status;
   nb.cell_kernel = g.nb_cell;
+  nb.struct_order = P->struct_order;
+  nb.smem_atoms = P->smem_atoms;
+  nb.smem_cells = P->smem_cells;
   return nb;
 }
 
@@ -2169,6 +2193,7 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     if (v == "cell") g.nb_cell = 1;
     else if (v == "stream") g.nb_cell = 2;
     else if (v == "half") g.nb_cell = 3;
+    else if (v == "struct") g.nb_cell = 4;
     else if (v == "atom") g.nb_cell = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;

@@ -230,9 +230,14 @@ struct NbBuffers {
   int* nb_img;                // optional: image T packed 3 x 10-bit signed
   unsigned* status;
   cudaEvent_t ev_search;      // optional: recorded right before the search kernel
+  // per-structure search (cell_kernel 4): structures largest first, and the
+  // shared-memory capacity of one block (atoms, cells); null = unavailable
+  const int* struct_order;
+  int smem_atoms, smem_cells;
   int cell_kernel;            // 0: warp per atom; warp per home cell with a lane per
                               // home atom (1) or a lane per candidate (2); 3: warp per
-                              // atom over the half stencil, each pair written to both rows
+                              // atom over the half stencil, each pair written to both rows;
+                              // 4: block per structure, cell lists in shared memory
 };
 
 int ae_launch_neighbors(int natoms, const double* pos, const int* types,

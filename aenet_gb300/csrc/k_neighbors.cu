@@ -204,16 +204,68 @@ struct VecOut<double4_32a> {
   static constexpr bool fp64 = true;
 };
 
+// The reference's FP64 predicate |L (s_j + T) - L s_i|^2 <= (Rc + 1e-3)^2,
+// unfused as lclist.f90 evaluates it, for FP32 distances too close to the
+// cut-off to decide (out of line: rarely taken, so the search loop keeps
+// its registers).
+__device__ __noinline__ bool band_fp64(const NbBuffers& nb, const StructGeom* g, int pbc,
+                                       bool self_img, int img, int i, int j, double rc2) {
+  const int oT0 = sext10i(img & 1023), oT1 = sext10i((img >> 10) & 1023),
+            oT2 = sext10i((img >> 20) & 1023);
+  double e2;
+  if (pbc) {
+    double cart[3];
+    if (self_img) {
+      for (int c = 0; c < 3; ++c) {
+        double t = dm(g->L[c], (double)oT0);
+        t = da(t, dm(g->L[3 + c], (double)oT1));
+        t = da(t, dm(g->L[6 + c], (double)oT2));
+        cart[c] = t;
+      }
+    } else {
+      const double* sj = nb.s_wrap + 3 * j;
+      double u0 = da(sj[0], (double)oT0), u1 = da(sj[1], (double)oT1),
+             u2 = da(sj[2], (double)oT2);
+      for (int c = 0; c < 3; ++c) {
+        double t = dm(g->L[c], u0);
+        t = da(t, dm(g->L[3 + c], u1));
+        t = da(t, dm(g->L[6 + c], u2));
+        cart[c] = da(t, -nb.r_wrap[3 * i + c]);
+      }
+    }
+    e2 = da(da(dm(cart[0], cart[0]), dm(cart[1], cart[1])), dm(cart[2], cart[2]));
+  } else {
+    double c0d = da(nb.r_wrap[3 * j], -nb.r_wrap[3 * i]);
+    double c1d = da(nb.r_wrap[3 * j + 1], -nb.r_wrap[3 * i + 1]);
+    double c2d = da(nb.r_wrap[3 * j + 2], -nb.r_wrap[3 * i + 2]);
+    e2 = da(da(dm(c0d, c0d), dm(c1d, c1d)), dm(c2d, c2d));
+  }
+  return e2 <= rc2;
+}
+
+// stencil units per lane in one round of the search (a round holds
+// 32 NB_UPL units; the stencils of the batch workloads need at most 125)
+constexpr int NB_UPL = 1;
+#ifndef NB_STRUCT_BLOCKS
+#define NB_STRUCT_BLOCKS 4
+#endif
+
+// Where a search reads the cell lists: the global arrays, or one
+// structure's copy in shared memory (cell-ordered entries p at p - base).
+struct CellSrc {
+  const int* cstart;     // cell_start of the structure's cells
+  const float4* cpos;    // cell-ordered positions (species bits in w)
+  const int* catoms;     // cell-ordered atom indices
+  int base;
+};
+
+// The neighbour row of atom i (one warp): the stencil walked as units,
+// candidates flattened 32 at a time, FP32 filter + FP64 band predicate,
+// accepted pairs compacted with ballots into the atom's ELL row.
 template <typename T4>
-__global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) {
-  __shared__ int su_base[8][32];      // per warp: cell_atoms offset of each unit
-  __shared__ float4 su_sh[8][32];     // image shift and packed image of each unit
-  __shared__ int su_first[8][32];     // unit starting at each offset of a batch
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= natoms) return;
-  const StructGeom* g = nb.geom + nb.atom_struct[i];
+__device__ __forceinline__ void search_atom(int i, const NbBuffers& nb, const StructGeom* g,
+                                            const CellSrc& src, int* su_base_w, float4* su_sh_w,
+                                            int* su_first_w, int lane) {
   const int pbc = g->pbc;
   const int nc0 = g->nc[0], nc1 = g->nc[1], nc2 = g->nc[2];
   const int k0 = g->kr[0], k1 = g->kr[1], k2 = g->kr[2];
@@ -230,7 +282,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
   const double rc2 = g->rc2;
   const int cap = nb.cap;
   const size_t row = (size_t)i * cap;
-  const int* __restrict__ cstart = nb.cell_start + g->cell_off;
+  const int* __restrict__ cstart = src.cstart;
   // lattice coordinates of the atom (pruning in orthogonal cells; the cut
   // is widened slightly so that rounding can only keep extra candidates)
   const float sf0 = (float)nb.s_wrap[3 * i], sf1 = (float)nb.s_wrap[3 * i + 1],
@@ -238,102 +290,134 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
   const float rcf = g->rcf * 1.0001f + 1e-4f;
   int cnt = 0;
 
-  const float inv_nt2 = __fdividef(1.0f, (float)nt2), inv_w1 = __fdividef(1.0f, (float)w1);
+  // u / nt2 and r / w1 by multiplication with 2^16 / n rounded up: exact
+  // for the unit counts of a stencil (u * n < 2^16)
+  const int m_nt2 = (65536 + nt2 - 1) / nt2, m_w1 = (65536 + w1 - 1) / w1;
   const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
   // geometry in registers: the table stores below may alias g as far as
   // the compiler knows, which would otherwise reload these every unit
   const int ortho = g->ortho;
   const float hf0 = g->hf[0], hf1 = g->hf[1], ihf2 = g->inv_hf[2];
   const float* __restrict__ Lf = g->Lf;
-  for (int ubase = 0; ubase < nunits; ubase += 32) {
-    // ---- this lane's unit: cells [zlo, zhi] of row (d0, d1), image t2
-    const int u = ubase + lane;
-    int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
-    float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
-    if (u < nunits) {
-      const int rr = floor_div_r(u, inv_nt2);
-      const int it2 = u - rr * nt2;
-      const int q0 = floor_div_r(rr, inv_w1);
-      const int d1 = rr - q0 * w1 - k1;
-      const int d0 = q0 - k0;
-      int a0 = c0 + d0, a1 = c1 + d1;
-      bool ok = true;
-      int zlo = c2 - k2, zhi = c2 + k2;   // unwrapped cell indices
-      if (ortho) {
-        const float x0 = (float)a0 * inc0, x1 = (float)(a0 + 1) * inc0;
-        const float y0 = (float)a1 * inc1, y1 = (float)(a1 + 1) * inc1;
-        const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * hf0;
-        const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * hf1;
-        const float rem = rcf * rcf - gx * gx - gy * gy;
-        if (rem < 0.f) {
-          ok = false;
+  for (int ubase = 0; ubase < nunits; ubase += 32 * NB_UPL) {
+    // ---- this lane's units ubase + NB_UPL lane + k: cells [zlo, zhi] of
+    // row (d0, d1), image t2; consecutive candidate ranges per lane
+    int lens[NB_UPL], starts[NB_UPL];
+    int mylen = 0;
+    __syncwarp();   // the previous round's readers are done
+#pragma unroll
+    for (int kk = 0; kk < NB_UPL; ++kk) {
+      const int u = ubase + NB_UPL * lane + kk;
+      int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0;
+      float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
+      if (u < nunits) {
+        const int rr = (u * m_nt2) >> 16;
+        const int it2 = u - rr * nt2;
+        const int q0 = (rr * m_w1) >> 16;
+        const int d1 = rr - q0 * w1 - k1;
+        const int d0 = q0 - k0;
+        int a0 = c0 + d0, a1 = c1 + d1;
+        bool ok = true;
+        int zlo = c2 - k2, zhi = c2 + k2;   // unwrapped cell indices
+        if (ortho) {
+          const float x0 = (float)a0 * inc0, x1 = (float)(a0 + 1) * inc0;
+          const float y0 = (float)a1 * inc1, y1 = (float)(a1 + 1) * inc1;
+          const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * hf0;
+          const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * hf1;
+          const float rem = rcf * rcf - gx * gx - gy * gy;
+          if (rem < 0.f) {
+            ok = false;
+          } else {
+            const float hz = sqrtf(rem) * ihf2 * 1.0001f + 1e-6f;
+            zlo = max(zlo, __float2int_rd((sf2 - hz) * nc2));
+            zhi = min(zhi, __float2int_rd((sf2 + hz) * nc2));
+          }
+        }
+        if (pbc) {
+          // images of the row's cell: a0, a1 lie within k of the home cell
+          while (a0 < 0) {
+            a0 += nc0;
+            --T0;
+          }
+          while (a0 >= nc0) {
+            a0 -= nc0;
+            ++T0;
+          }
+          while (a1 < 0) {
+            a1 += nc1;
+            --T1;
+          }
+          while (a1 >= nc1) {
+            a1 -= nc1;
+            ++T1;
+          }
+          T2 = t2lo + it2;
+          zlo = max(zlo, T2 * nc2);
+          zhi = min(zhi, T2 * nc2 + nc2 - 1);
         } else {
-          const float hz = sqrtf(rem) * ihf2 * 1.0001f + 1e-6f;
-          zlo = max(zlo, (int)floorf((sf2 - hz) * nc2));
-          zhi = min(zhi, (int)floorf((sf2 + hz) * nc2));
+          ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
+          zlo = max(zlo, 0);
+          zhi = min(zhi, nc2 - 1);
+        }
+        if (ok && zlo <= zhi) {
+          const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
+          beg = cstart[base + zlo];
+          len = cstart[base + zhi + 1] - beg;
+          const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
+          sh0 = f0 * Lf[0] + f1 * Lf[3] + f2 * Lf[6];
+          sh1 = f0 * Lf[1] + f1 * Lf[4] + f2 * Lf[7];
+          sh2 = f0 * Lf[2] + f1 * Lf[5] + f2 * Lf[8];
         }
       }
-      if (pbc) {
-        T0 = floor_div_r(a0, inc0);
-        a0 -= T0 * nc0;
-        T1 = floor_div_r(a1, inc1);
-        a1 -= T1 * nc1;
-        T2 = t2lo + it2;
-        zlo = max(zlo, T2 * nc2);
-        zhi = min(zhi, T2 * nc2 + nc2 - 1);
-      } else {
-        ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
-        zlo = max(zlo, 0);
-        zhi = min(zhi, nc2 - 1);
-      }
-      if (ok && zlo <= zhi) {
-        const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
-        beg = cstart[base + zlo];
-        len = cstart[base + zhi + 1] - beg;
-        const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
-        sh0 = f0 * Lf[0] + f1 * Lf[3] + f2 * Lf[6];
-        sh1 = f0 * Lf[1] + f1 * Lf[4] + f2 * Lf[7];
-        sh2 = f0 * Lf[2] + f1 * Lf[5] + f2 * Lf[8];
-      }
+      lens[kk] = len;
+      starts[kk] = mylen;   // offset inside this lane's range for now
+      mylen += len;
+      su_base_w[NB_UPL * lane + kk] = beg - starts[kk];   // minus the lane's start below
+      su_sh_w[NB_UPL * lane + kk] = make_float4(
+          sh0, sh1, sh2, __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) | ((T2 & 1023) << 20)));
     }
-    int incl = len;
+    int incl = mylen;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const int w = __shfl_up_sync(0xffffffffu, incl, d);
       if (lane >= d) incl += w;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    // unit table of this round in shared memory: candidate q belongs to the
-    // unit whose start is the last start <= q
-    const int start = incl - len;
-    __syncwarp();   // the previous round's readers are done
-    su_base[warp][lane] = beg - start;   // cell_atoms index = base + q
-    su_sh[warp][lane] = make_float4(sh0, sh1, sh2,
-                                    __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) |
-                                                   ((T2 & 1023) << 20)));
+    const int lstart = incl - mylen;
+#pragma unroll
+    for (int kk = 0; kk < NB_UPL; ++kk) {
+      starts[kk] += lstart;
+      su_base_w[NB_UPL * lane + kk] -= lstart;   // cell_atoms index = base + q
+    }
     __syncwarp();
     int carry = 0;
     for (int qb = 0; qb < total; qb += 32) {
       const int q = qb + lane;
       // units starting inside this batch mark their offsets
-      const bool starts = len > 0 && start >= qb && start < qb + 32;
+      unsigned mine = 0u;
       __syncwarp();   // the previous batch's readers are done
-      if (starts) su_first[warp][start - qb] = lane;
-      const unsigned marks = __reduce_or_sync(0xffffffffu, starts ? (1u << (start - qb)) : 0u);
+#pragma unroll
+      for (int kk = 0; kk < NB_UPL; ++kk) {
+        if (lens[kk] > 0 && starts[kk] >= qb && starts[kk] < qb + 32) {
+          su_first_w[starts[kk] - qb] = NB_UPL * lane + kk;
+          mine |= 1u << (starts[kk] - qb);
+        }
+      }
+      const unsigned marks = __reduce_or_sync(0xffffffffu, mine);
       __syncwarp();
       const unsigned upto = marks & (0xffffffffu >> (31 - lane));
-      const int own = upto ? su_first[warp][31 - __clz(upto)] : carry;
+      const int own = upto ? su_first_w[31 - __clz(upto)] : carry;
       carry = __shfl_sync(0xffffffffu, own, 31);
-      const float4 osh = su_sh[warp][own];
+      const float4 osh = su_sh_w[own];
       const int img = __float_as_int(osh.w);   // packed image; zero for T = 0
       const float osh0 = osh.x, osh1 = osh.y, osh2 = osh.z;
       bool accept = false;
       int j = -1, tj = 0;
       float dx = 0.f, dy = 0.f, dz = 0.f, dd2 = 0.f;
       if (q < total) {
-        const int p = su_base[warp][own] + q;
-        const float4 rj = nb.cell_pos[p];
-        j = nb.cell_atoms[p];
+        const int p = su_base_w[own] + q;
+        const float4 rj = src.cpos[p - src.base];
+        j = src.catoms[p - src.base];
         tj = __float_as_int(rj.w);
         const bool self_img = (j == i);
         const bool zeroT = img == 0;
@@ -346,37 +430,7 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
             accept = true;
           } else if (dd2 <= rc2_hi) {
             // exact FP64 predicate, evaluated as the reference does
-            const int oT0 = sext10i(img & 1023), oT1 = sext10i((img >> 10) & 1023),
-                      oT2 = sext10i((img >> 20) & 1023);
-            double e2;
-            if (pbc) {
-              double cart[3];
-              if (self_img) {
-                for (int c = 0; c < 3; ++c) {
-                  double t = dm(g->L[c], (double)oT0);
-                  t = da(t, dm(g->L[3 + c], (double)oT1));
-                  t = da(t, dm(g->L[6 + c], (double)oT2));
-                  cart[c] = t;
-                }
-              } else {
-                const double* sj = nb.s_wrap + 3 * j;
-                double u0 = da(sj[0], (double)oT0), u1 = da(sj[1], (double)oT1),
-                       u2 = da(sj[2], (double)oT2);
-                for (int c = 0; c < 3; ++c) {
-                  double t = dm(g->L[c], u0);
-                  t = da(t, dm(g->L[3 + c], u1));
-                  t = da(t, dm(g->L[6 + c], u2));
-                  cart[c] = da(t, -nb.r_wrap[3 * i + c]);
-                }
-              }
-              e2 = da(da(dm(cart[0], cart[0]), dm(cart[1], cart[1])), dm(cart[2], cart[2]));
-            } else {
-              double c0d = da(nb.r_wrap[3 * j], -nb.r_wrap[3 * i]);
-              double c1d = da(nb.r_wrap[3 * j + 1], -nb.r_wrap[3 * i + 1]);
-              double c2d = da(nb.r_wrap[3 * j + 2], -nb.r_wrap[3 * i + 2]);
-              e2 = da(da(dm(c0d, c0d), dm(c1d, c1d)), dm(c2d, c2d));
-            }
-            accept = (e2 <= rc2);
+            accept = band_fp64(nb, g, pbc, self_img, img, i, j, rc2);
           }
         }
       }
@@ -421,6 +475,49 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
     nb.nb_cnt[i] = min(cnt, cap);
     if (cnt > cap) atomicOr(nb.status, AE_ST_NB_OVERFLOW);
   }
+}
+
+template <typename T4>
+__global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) {
+  __shared__ int su_base[8][32 * NB_UPL];      // per warp: cell_atoms offset of each unit
+  __shared__ float4 su_sh[8][32 * NB_UPL];     // image shift and packed image of each unit
+  __shared__ int su_first[8][32];              // unit starting at each offset of a batch
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= natoms) return;
+  const StructGeom* g = nb.geom + nb.atom_struct[i];
+  const CellSrc src{nb.cell_start + g->cell_off, nb.cell_pos, nb.cell_atoms, 0};
+  search_atom<T4>(i, nb, g, src, su_base[warp], su_sh[warp], su_first[warp], lane);
+}
+
+// One block per structure (structures in the order nb.struct_order, largest
+// first): the structure's cell-ordered positions, atom indices and cell
+// offsets are staged in shared memory, then the block's warps take its
+// atoms one by one with the same search.
+template <typename T4>
+__global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS) k_neighbors_struct(NbBuffers nb) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  __shared__ int su_base[8][32 * NB_UPL];
+  __shared__ float4 su_sh[8][32 * NB_UPL];
+  __shared__ int su_first[8][32];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const StructGeom* g = nb.geom + nb.struct_order[blockIdx.x];
+  const int n = g->natoms, a0 = g->atom_off;
+  const int ncell = g->nc[0] * g->nc[1] * g->nc[2];
+  float4* spos = reinterpret_cast<float4*>(sm_raw);
+  int* satoms = reinterpret_cast<int*>(spos + nb.smem_atoms);
+  int* scs = satoms + nb.smem_atoms;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    spos[q] = nb.cell_pos[a0 + q];
+    satoms[q] = nb.cell_atoms[a0 + q];
+  }
+  for (int q = threadIdx.x; q <= ncell; q += blockDim.x) scs[q] = nb.cell_start[g->cell_off + q];
+  __syncthreads();
+  const CellSrc src{scs, spos, satoms, a0};
+  for (int a = warp; a < n; a += (blockDim.x >> 5))
+    search_atom<T4>(a0 + a, nb, g, src, su_base[warp], su_sh[warp], su_first[warp], lane);
 }
 
 // ---- cell-batched search: one warp per home cell, lane h = home atom h.
@@ -903,8 +1000,8 @@ constexpr int AE_HOME_UNIT = 1 << 30;   // unit flag beside the packed image
 
 template <typename T4>
 __global__ void __launch_bounds__(256, 4) k_neighbors_half(int natoms, NbBuffers nb) {
-  __shared__ int su_base[8][32];
-  __shared__ float4 su_sh[8][32];
+  __shared__ int su_base[8][32 * NB_UPL];
+  __shared__ float4 su_sh[8][32 * NB_UPL];
   __shared__ int su_first[8][32];
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -1199,6 +1296,21 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
   k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
   k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
   if (nb.ev_search) cudaEventRecord(nb.ev_search, s);
+  if (nb.cell_kernel == 4 && nb.struct_order) {
+    const size_t smem = 20 * (size_t)nb.smem_atoms + 4 * ((size_t)nb.smem_cells + 1);
+    if (fp64) {
+      auto kern = k_neighbors_struct<double4_32a>;
+      if (smem + 24576 > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<nb.nstruc, 256, smem, s>>>(nb);
+    } else {
+      auto kern = k_neighbors_struct<float4>;
+      if (smem + 24576 > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<nb.nstruc, 256, smem, s>>>(nb);
+    }
+    return (int)cudaGetLastError();
+  }
   if (nb.cell_kernel == 3) {
     e = cudaMemsetAsync(nb.nb_cnt, 0, sizeof(int) * (size_t)natoms, s);
     if (e != cudaSuccess) return (int)e;
@@ -1218,7 +1330,7 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
       k_neighbors_stream<float4><<<blocks, 32 * NBS_WARPS, 0, s>>>(nc, nb);
     return (int)cudaGetLastError();
   }
-  if (nb.cell_kernel) {
+  if (nb.cell_kernel == 1) {
     const int blocks = (nc + NBC_WARPS - 1) / NBC_WARPS;
     if (fp64)
       k_neighbors_cell<double4_32a><<<blocks, 32 * NBC_WARPS, 0, s>>>(nc, nb);

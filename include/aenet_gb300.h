@@ -48,14 +48,18 @@ extern "C" {
  *       atom (performance only).
  *   "adjoint_lanes_per_atom" = "0" | "8" | "16" | "32"   the same for the
  *       adjoint kernels; 0 follows lanes_per_atom (performance only).
- *   "neighbour_kernel" = "atom" | "cell" | "stream" | "half"   neighbour
+ *   "neighbour_kernel" = "atom" | "cell" | "stream" | "half" | "struct"   neighbour
  *       search with one warp per atom (pruned per atom), one warp per home
  *       cell with a lane per home atom (dense cells of large structures),
  *       one warp per home cell with a lane per candidate, each batch of
  *       candidates tested against every home atom (few atoms per cell), or
  *       one warp per atom over half the stencil, each pair found once and
  *       written to both rows (the order inside a row then varies from run
- *       to run); same neighbour sets (performance only).
+ *       to run), or one block per structure with the structure's cell
+ *       lists staged in shared memory and warps taking its atoms in turn
+ *       (batches of small structures; plans whose largest structure does
+ *       not fit a block use the warp-per-atom search); same neighbour sets
+ *       (performance only).
  *   "networks" = "tensor" | "simt"   mixed-path networks on the tcgen05
  *       tensor cores (split BF16, FP32 accumulation; networks with two
  *       hidden layers and widths up to 64) or on FP32 SIMT.

@@ -49,7 +49,8 @@ def aucu(oracle, tmp_path_factory):
     return w, paths
 
 
-@pytest.fixture(params=["atom", "cell", "stream", "half", "atom_z4", "stream_z2", "half_z4"])
+@pytest.fixture(params=["atom", "cell", "stream", "half", "struct", "atom_z4", "stream_z2",
+                        "half_z4", "struct_z4"])
 def nb_kernel(request, cuda):
     """Run a test with each neighbour-search kernel (one warp per atom over
     the full or the half stencil, or one warp per home cell with a lane per

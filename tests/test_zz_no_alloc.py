@@ -46,7 +46,11 @@ def setup(oracle, tmp_path_factory):
     sub.networks = w.networks
     paths = helpers.make_potentials(oracle, sub, str(tmp_path_factory.mktemp("noalloc")))
     ann = ANNPotentials({t: paths[t] for t in w.types})
-    yield torch, ann, sub.structures[0]
+    # the allocation-free call reads the device tables that the first
+    # allocating evaluation builds
+    st = sub.structures[0]
+    ann.structure_energy_forces(st.positions, st.types, st.cell)
+    yield torch, ann, st
     ann.release()
 
 
