@@ -379,17 +379,26 @@ __global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_FWD_BLOCKS : 3) : 
     accs[q] = T(0);
   }
   int na = 0;
+  // the table row is read one iteration ahead (its load latency overlaps
+  // the previous neighbour's work)
+  T4 vn;
+  int qn = 0;
+  if (sl < n) {
+    vn = vec[sl];
+    qn = jt[sl];
+  }
   for (int base = 0; base < nloop; base += LPA) {
     const int j = base + sl;
     const bool valid = j < n;
-    T4 v;
-    int t = 0;
-    if (valid) {
-      v = vec[j];
-      t = jt[j] >> AE_TYPE_SHIFT;
-    } else {
+    T4 v = vn;
+    const int t = valid ? (qn >> AE_TYPE_SHIFT) : 0;
+    if (!valid) {
       v.x = v.y = v.z = T(0);
       v.w = T(1e30);
+    }
+    if (j + LPA < n) {
+      vn = vec[j + LPA];
+      qn = jt[j + LPA];
     }
     const T d = v.w;
     const T s = multi ? T(s_spin[ti * AE_MAXT + t]) : T(0);
@@ -591,19 +600,28 @@ __global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_ADJ_BLOCKS : 3)
   T fix = T(0), fiy = T(0), fiz = T(0);
   T w00 = 0, w01 = 0, w02 = 0, w10 = 0, w11 = 0, w12 = 0, w20 = 0, w21 = 0, w22 = 0;
   int na = 0;
+  // the table row is read one iteration ahead, as in the forward
+  T4 vn;
+  int qn = 0;
+  if (sl < n) {
+    vn = vec[sl];
+    qn = jt[sl];
+  }
   for (int base = 0; base < nloop; base += LPA) {
     const int j = base + sl;
     const bool valid = j < n;
-    T4 v;
+    T4 v = vn;
     int t = 0, jatom = 0;
     if (valid) {
-      v = vec[j];
-      const int q = jt[j];
-      t = q >> AE_TYPE_SHIFT;
-      jatom = q & AE_INDEX_MASK;
+      t = qn >> AE_TYPE_SHIFT;
+      jatom = qn & AE_INDEX_MASK;
     } else {
       v.x = v.y = v.z = T(0);
       v.w = T(1e30);
+    }
+    if (j + LPA < n) {
+      vn = vec[j + LPA];
+      qn = jt[j + LPA];
     }
     const T d = v.w;
     const T s = multi ? T(s_spin[ti * AE_MAXT + t]) : T(0);

@@ -57,14 +57,25 @@ __global__ void __launch_bounds__(128) k_tangent(PotDevice pd, DescBuffers b) {
 #pragma unroll
   for (int q = 0; q < R; ++q) acc[q] = accs[q] = T(0);
   int na = 0;
+  // the table row is read one iteration ahead (its load latency overlaps
+  // the previous neighbour's work)
+  T4 vn;
+  int qn = 0;
+  if (sl < n) {
+    vn = vec[sl];
+    qn = jt[sl];
+  }
   for (int base = 0; base < nloop; base += LPA) {
     const int j = base + sl;
     const bool valid = j < n;
-    T4 v, dlt;
+    T4 v = vn, dlt;
+    const int q = qn;
     int t = 0;
+    if (j + LPA < n) {
+      vn = vec[j + LPA];
+      qn = jt[j + LPA];
+    }
     if (valid) {
-      v = vec[j];
-      const int q = jt[j];
       t = q >> AE_TYPE_SHIFT;
       const T4 uj = U[q & AE_INDEX_MASK];
       dlt.x = uj.x - ui.x;
@@ -275,14 +286,25 @@ __global__ void __launch_bounds__(128, A <= 5 ? AE_TAN_MOM_BLOCKS : 3) k_tangent
 #pragma unroll
   for (int q = 0; q < R; ++q) acc[q] = accs[q] = T(0);
   int na = 0;
+  // the table row is read one iteration ahead (its load latency overlaps
+  // the previous neighbour's work)
+  T4 vn;
+  int qn = 0;
+  if (sl < n) {
+    vn = vec[sl];
+    qn = jt[sl];
+  }
   for (int base = 0; base < nloop; base += LPA) {
     const int j = base + sl;
     const bool valid = j < n;
-    T4 v, dlt;
+    T4 v = vn, dlt;
+    const int q = qn;
     int t = 0;
+    if (j + LPA < n) {
+      vn = vec[j + LPA];
+      qn = jt[j + LPA];
+    }
     if (valid) {
-      v = vec[j];
-      const int q = jt[j];
       t = q >> AE_TYPE_SHIFT;
       const T4 uj = U[q & AE_INDEX_MASK];
       dlt.x = uj.x - ui.x;
