@@ -126,6 +126,9 @@ def _declare(lib):
     lib.aenet_gpu_md_get.restype = C.c_int
     lib.aenet_gpu_md_counters.argtypes = [vp, C.POINTER(C.c_longlong), ip]
     lib.aenet_gpu_md_counters.restype = C.c_int
+    lib.aenet_gpu_md_phase_times.argtypes = [vp, dp, C.POINTER(C.c_longlong), dp,
+                                             C.POINTER(C.c_longlong)]
+    lib.aenet_gpu_md_phase_times.restype = C.c_int
     lib.aenet_gpu_md_energy_fp64.argtypes = [vp, dp]
     lib.aenet_gpu_md_energy_fp64.restype = C.c_int
     return lib

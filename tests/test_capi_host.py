@@ -149,3 +149,21 @@ def test_noalloc_entry_point_requires_loaded_tables():
     rc = lib.aenet_gpu_structure_energy_forces_noalloc(
         4, fake, fake, lat.ctypes.data_as(C.c_void_p), 0, None, None, None, None, None)
     assert rc == 1
+
+
+def test_every_declared_function_has_ctypes_signature():
+    """Each function of include/*.h is bound with argtypes in the ctypes
+    layer: without them ctypes passes Python ints (handles, pointers) as
+    32-bit C ints, which truncates pointers above 4 GB."""
+    import ctypes as C
+    import os
+    import re
+    from aenet_gb300 import _lib
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    text = "".join(open(os.path.join(root, "include", h)).read()
+                   for h in ("aenet.h", "aenet_gb300.h"))
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = sorted(set(re.findall(r"\b(aenet_\w+)\s*\(", text)))
+    lib = _lib._declare(C.CDLL(_lib.LIB_PATH))
+    missing = [n for n in names if getattr(lib, n).argtypes is None]
+    assert not missing, missing
