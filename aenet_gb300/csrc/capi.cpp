@@ -1219,7 +1219,14 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
     max_n = std::max(max_n, P->natoms_h[s]);
     max_c = std::max(max_c, P->geom_h[s].nc[0] * P->geom_h[s].nc[1] * P->geom_h[s].nc[2]);
   }
-  const bool per_struct = 20 * (size_t)max_n + 4 * ((size_t)max_c + 1) + 24576 <= 48 * 1024;
+  // and there are enough structures to give every SM a few blocks (fewer,
+  // larger structures spread better one warp per atom)
+  int nsm = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    nsm = 0;
+  const bool per_struct = nsm > 0 && P->nstruc >= 2 * nsm &&
+                          20 * (size_t)max_n + 4 * ((size_t)max_c + 1) + 24576 <= 48 * 1024;
   size_t o_so2 = per_struct ? take(4 * (size_t)P->nstruc) : 0;
   if (cudaMalloc(&P->mem, off) != cudaSuccess) return AENET_ERR_CUDA;
   P->mem_bytes = off;

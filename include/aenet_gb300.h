@@ -57,9 +57,10 @@ extern "C" {
  *       written to both rows (the order inside a row then varies from run
  *       to run), or one block per structure with the structure's cell
  *       lists staged in shared memory and warps taking its atoms in turn
- *       (batches of small structures; plans whose largest structure does
- *       not fit a block use the warp-per-atom search); same neighbour sets
- *       (performance only).
+ *       (batches of small structures; plans with fewer structures than
+ *       twice the SMs, or whose largest structure does not fit a block,
+ *       use the warp-per-atom search); same neighbour sets (performance
+ *       only).
  *   "networks" = "tensor" | "simt"   mixed-path networks on the tcgen05
  *       tensor cores (split BF16, FP32 accumulation; networks with two
  *       hidden layers and widths up to 64) or on FP32 SIMT.

@@ -855,3 +855,49 @@ def test_per_atom_calls_reuse_their_buffers(cuda, oracle, cu256):
                     first[key] = (e, F)
     finally:
         ann.release()
+
+
+def test_per_structure_search_matches_per_atom_search(cuda, oracle, tmp_path):
+    """The block-per-structure search (taken for batches of more than twice
+    as many structures as SMs) against the warp-per-atom search on 320
+    small cells: identical (neighbour, image) sets per row, in both
+    precisions, on the plain and the refined grid; FP64 energies equal to
+    rounding and against the oracle on a sample of cells."""
+    torch = cuda
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import FP64, MIXED, set_option
+    from aenet_gb300.plan import Plan
+    w = workloads.lisio_batch_4096(nstruc=320)
+    paths = helpers.make_potentials(oracle, w, str(tmp_path), max_atoms=500)
+    ann = _ann(paths, w.types)
+    try:
+        nat, pos, typ, cells, pbc = w.packed()
+        p = torch.tensor(pos, device="cuda")
+        t = torch.tensor(typ, device="cuda")
+        for z in (1, 4):
+            set_option("z_refine", z)
+            for prec in (FP64, MIXED):
+                got = {}
+                for kern in ("atom", "struct"):
+                    set_option("neighbour_kernel", kern)
+                    plan = Plan(nat, cells, pbc, precision=prec)
+                    o = plan.run(p, t)
+                    plan.check()
+                    got[kern] = _neighbour_keys(torch, plan, p, cells, nat) + (o["E"].clone(),)
+                    plan.close()
+                a, s = got["atom"], got["struct"]
+                assert torch.equal(a[0], s[0])
+                assert torch.equal(a[1], s[1])
+                tol = 1e-11 if prec == FP64 else 1e-5
+                assert ((a[4] - s[4]).abs() / torch.as_tensor(nat, device="cuda")).max() < tol
+                if prec == FP64 and z == 4:
+                    E = s[4].cpu().numpy()
+        oracle.load(w.types, paths)
+        for k in (0, 7, 160, 319):
+            st = w.structures[k]
+            _, et, _, _ = oracle.structure(st.cell, st.positions, st.types)
+            assert abs(E[k] - et) / st.natoms < E_TOL_FP64, k
+    finally:
+        set_option("neighbour_kernel", "atom")
+        set_option("z_refine", 1)
+        ann.release()
