@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libaenet_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["k_neighbors.cu", "k_cheb_order.cu", "k_cheb_f32.cu", "k_cheb_mom.cu", "k_cheb_f64.cu", "k_behler.cu", "k_mlp.cu", "k_mlp_tc.cu",
+SOURCES = ["k_neighbors.cu", "k_cheb_order.cu", "k_atom.cu", "k_cheb_f32.cu", "k_cheb_mom.cu", "k_cheb_f64.cu", "k_behler.cu", "k_mlp.cu", "k_mlp_tc.cu",
            "k_cheb_tangent.cu", "k_cheb_jac.cu", "k_train.cu", "k_md.cu", "capi.cpp", "noalloc.cu"]
 
 

@@ -69,7 +69,7 @@ def _i32(a):
 def set_option(key, value):
     """aenet_gpu_set_option: angular_domain, angular_spin, angular_terms,
     cell_div, z_refine, lanes_per_atom, adjoint_lanes_per_atom,
-    neighbour_kernel, networks (include/aenet_gb300.h)."""
+    neighbour_kernel, networks, per_atom_kernel (include/aenet_gb300.h)."""
     st = _lib.lib().aenet_gpu_set_option(key.encode(), str(value).encode())
     check_status(st)
 

@@ -275,6 +275,8 @@ struct State {
                              // warp per atom over the half stencil (3)
   int angular_moments = 1;   // FP32 angular terms in moment form where instantiated
   int angular_spin_stale = 0;  // Chebyshev spin block with sfb_eval's stale s_j
+  int atom_fused = 1;          // per-atom calls: one fused launch (1) or the graph of the
+                               // batch kernels (0)
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
@@ -1602,6 +1604,9 @@ struct AtomScratch {
   size_t host_bytes = 0;
   cudaStream_t stream = nullptr;
   std::vector<AtomGraph> graphs;
+  char* mhost = nullptr;   // mapped pinned block of the fused per-atom launch
+  char* mdev = nullptr;    // its device address
+  size_t mbytes = 0;
   void drop_graphs() {
     for (auto& q : graphs) cudaGraphExecDestroy(q.exec);
     graphs.clear();
@@ -1638,6 +1643,65 @@ int atom_scratch_reserve(size_t dev_bytes, size_t host_bytes) {
   return 0;
 }
 
+int atom_mapped_reserve(size_t bytes) {
+  if (!g_atom.stream && cudaStreamCreateWithFlags(&g_atom.stream, cudaStreamNonBlocking))
+    return AENET_ERR_CUDA;
+  if (g_atom.mbytes >= bytes) return 0;
+  if (g_atom.mhost) cudaFreeHost(g_atom.mhost);
+  g_atom.mhost = g_atom.mdev = nullptr;
+  g_atom.mbytes = 0;
+  const size_t want = std::max(bytes, (size_t)1 << 16);
+  if (cudaHostAlloc((void**)&g_atom.mhost, want, cudaHostAllocMapped) != cudaSuccess) {
+    g_atom.mhost = nullptr;
+    return AENET_ERR_MALLOC;
+  }
+  if (cudaHostGetDevicePointer((void**)&g_atom.mdev, g_atom.mhost, 0) != cudaSuccess) {
+    cudaFreeHost(g_atom.mhost);
+    g_atom.mhost = g_atom.mdev = nullptr;
+    return AENET_ERR_CUDA;
+  }
+  g_atom.mbytes = want;
+  return 0;
+}
+
+// One FP64 Chebyshev atom in one launch of the fused per-atom kernel, the
+// row and the results in mapped host memory; AE_ATOM_NA when the potential
+// or the row does not fit that kernel.
+int atomic_eval_fused(const double* coo_i, int type_i, int n_j, const double* coo_j,
+                      const int* type_j, double* E_i, double* F_local) {
+  const size_t in_bytes =
+      ((size_t)AE_ATOM_IN_VEC + 36 * (size_t)n_j + 255) & ~(size_t)255;
+  const size_t out_bytes = AE_ATOM_OUT_F + 24 * (size_t)(n_j + 1);
+  int st = atom_mapped_reserve(in_bytes + out_bytes);
+  if (st) return st;
+  char* h = g_atom.mhost;
+  AtomCallHeader* hd = reinterpret_cast<AtomCallHeader*>(h);
+  hd->n = n_j;
+  hd->ti = type_i - 1;
+  hd->forces = F_local ? 1 : 0;
+  hd->pad = 0;
+  // R_ij = coo_j - coo_i (sfbasis.f90:488) and its length
+  double* vec = reinterpret_cast<double*>(h + AE_ATOM_IN_VEC);
+  int* ty = reinterpret_cast<int*>(h + AE_ATOM_IN_VEC + 32 * (size_t)n_j);
+  for (int j = 0; j < n_j; ++j) {
+    double R[3];
+    for (int c = 0; c < 3; ++c) R[c] = coo_j[3 * j + c] - coo_i[c];
+    vec[4 * j] = R[0];
+    vec[4 * j + 1] = R[1];
+    vec[4 * j + 2] = R[2];
+    vec[4 * j + 3] = std::sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
+    ty[j] = type_j[j] - 1;
+  }
+  const char* ho = h + in_bytes;
+  const int e = ae_launch_atom(g.pd, n_j, g_atom.mdev, g_atom.mdev + in_bytes, g_atom.stream);
+  if (e == AE_ATOM_NA) return AE_ATOM_NA;
+  if (e || cudaStreamSynchronize(g_atom.stream) != cudaSuccess) return AENET_ERR_CUDA;
+  if (*reinterpret_cast<const unsigned*>(ho + 8)) return AENET_ERR_CUDA;
+  *E_i = *reinterpret_cast<const double*>(ho);
+  if (F_local) memcpy(F_local, ho + AE_ATOM_OUT_F, 24 * (size_t)(n_j + 1));
+  return 0;
+}
+
 // One atom with caller-supplied neighbours, evaluated on the GPU as a
 // one-row neighbour table (aenet.f90:359-486).  F_local[(n_j+1)*3]
 // receives the forces on the central atom (row 0) and on each neighbour.
@@ -1655,6 +1719,10 @@ int atomic_eval(const double* coo_i, int type_i, int n_j, const double* coo_j, c
   const int cap = std::max(32, (n_j + 31) & ~31);
   const bool fp64 = true;
   const bool stale = stale_spin_wanted();
+  if (g.atom_fused && !stale && n_j <= AE_ATOM_NMAX) {
+    st = atomic_eval_fused(coo_i, type_i, n_j, coo_j, type_j, E_i, F_local);
+    if (st != AE_ATOM_NA) return st;
+  }
   const size_t nsf_pad = pd.nsf_pad;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -2208,6 +2276,12 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
   if (k == "angular_terms") {
     if (v == "moments") g.angular_moments = 1;
     else if (v == "pairs") g.angular_moments = 0;
+    else return AENET_ERR_INPUT;
+    return AENET_OK;
+  }
+  if (k == "per_atom_kernel") {
+    if (v == "fused") g.atom_fused = 1;
+    else if (v == "graph") g.atom_fused = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;
   }

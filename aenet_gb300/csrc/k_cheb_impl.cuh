@@ -893,8 +893,11 @@ __global__ void __launch_bounds__(128, MOM ? (A <= 5 ? AE_MOM_ADJ_BLOCKS : 3)
 
 template <typename T, int R, int A, int LPA, bool GUARD, bool MOM>
 int launch(const PotDevice& pd, const DescBuffers& b, bool adjoint, cudaStream_t s) {
-  const int warps = 4;
-  const int groups = warps * (32 / LPA);
+  // four warps per block, fewer when the atoms do not fill them (the
+  // per-atom calls: one group, so long rows still fit shared memory)
+  const int gpw = 32 / LPA;
+  const int warps = b.natoms >= 4 * gpw ? 4 : (b.natoms + gpw - 1) / gpw;
+  const int groups = warps * gpw;
   size_t scratch = 0;
   if constexpr (MOM) scratch = adjoint ? 0 : mom_scratch_bytes<A, LPA>();
   size_t smem = group_smem_bytes<T>(b.cap_a, pd.nsf_pad, adjoint, scratch) * groups;

@@ -14,6 +14,7 @@
 // normalisation scale 1/s (sfsetup.f90:1010-1031): the adjoint kernels
 // contract it with the derivatives of the raw descriptor.
 #include "common.h"
+#include "activate.cuh"
 
 namespace {
 
@@ -22,25 +23,6 @@ __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
   return v;
-}
-
-__device__ __forceinline__ float tanh_t(float x) { return tanhf(x); }
-__device__ __forceinline__ double tanh_t(double x) { return tanh(x); }
-__device__ __forceinline__ float exp_t(float x) { return expf(x); }
-__device__ __forceinline__ double exp_t(double x) { return exp(x); }
-
-// ff_activate: feedforward.f90:932-969
-template <typename T>
-__device__ __forceinline__ void activate(int t, T x, T& y, T& dy) {
-  const T a = T(1.7159), b = T(0.666666666666667), c = T(0.1);
-  switch (t) {
-    case 0: y = x; dy = T(1); break;
-    case 1: y = tanh_t(x); dy = T(1) - y * y; break;
-    case 2: y = T(1) / (T(1) + exp_t(-x)); dy = y * (T(1) - y); break;
-    case 3: { T tb = tanh_t(b * x); y = a * tb; dy = a * (T(1) - tb * tb) * b; } break;
-    case 4: { T tb = tanh_t(b * x); y = a * tb + c * x; dy = a * (T(1) - tb * tb) * b + c; } break;
-    default: y = T(0); dy = T(0);
-  }
 }
 
 template <typename T>

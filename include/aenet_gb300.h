@@ -82,6 +82,14 @@ extern "C" {
  *       Pair form only (the moment form is skipped); applies to plans
  *       created afterwards; the force term of the training loss and the
  *       descriptor Jacobians need "own" (AENET_ERR_INPUT otherwise).
+ *   "per_atom_kernel" = "fused" | "graph"   aenet_atomic_energy(_and_forces)
+ *       on Chebyshev potentials (orders up to 24 radial, 16 angular; up to
+ *       512 neighbours; angular_spin own): one block evaluates the call in
+ *       one launch, the row read from and the results written to mapped
+ *       host memory (fused), or the batch kernels run on a one-row table
+ *       from a captured graph (graph; also what Behler potentials, stale
+ *       spins and longer rows always take).  Same results to FP64
+ *       rounding.
  * Returns AENET_OK or AENET_ERR_INPUT.  "cell_div" and "z_refine" apply to
  * plans created afterwards, "angular_domain" from the next evaluation (the
  * device tables are rebuilt), the others from the next launch. */

@@ -828,6 +828,90 @@ def test_stale_spin_option_matches_oracle(cuda, oracle, tmp_path):
     assert np.abs(own["atomic_energies"] - Ea_or).max() > 1e-6
 
 
+@pytest.mark.parametrize("angular", ["current", "legacy"])
+def test_fused_per_atom_kernel_matches_oracle_and_graph_path(cuda, oracle, aucu, angular,
+                                                              tmp_path):
+    """The fused per-atom launch (one block per call, FP64) against the
+    oracle and against the graph of the batch kernels (per_atom_kernel =
+    graph): two species with the spin block, both angular domains, rows of
+    the alloy cell (about 80 neighbours, 24 angular), rows of a dense
+    random cell (over 300 neighbours, about 110 angular: several staging
+    chunks and pair rounds), a row beyond the fused kernel's 512
+    neighbours (taken by the graph path), one neighbour and none;
+    energy-only calls give the same energy; repeated calls the same bits."""
+    from aenet_gb300 import workloads
+    from aenet_gb300.core import set_option
+    w, paths = aucu
+    s0 = w.structures[0]
+    sites, _ = workloads.fcc_positions(10, 3.90)
+    keep = np.all(sites < 3 * 3.90 - 0.1, axis=1)
+    s = workloads.Structure(s0.positions[keep], s0.types[keep], np.eye(3) * (3 * 3.90))
+    # a dense random cell (0.3 atoms/A^3, ~340 neighbours and ~110 angular
+    # ones per atom) with a potential normalised on it, so that its rows
+    # reach real forces
+    rng = np.random.default_rng(7)
+    box = 12.0
+    pts = np.zeros((0, 3))
+    while len(pts) < int(0.3 * box ** 3):
+        p = rng.random(3) * box
+        if len(pts) == 0 or np.linalg.norm((p - pts + box / 2) % box - box / 2, axis=1).min() > 0.9:
+            pts = np.vstack([pts, p])
+    dense = workloads.Structure(pts, 1 + rng.integers(0, 2, len(pts)), np.eye(3) * box)
+    wd = workloads.Workload("dense", w.types, w.setups, w.arch, [dense], 11)
+    wd.networks = workloads.glorot_networks(rng, w.types, w.arch)
+    dpaths = helpers.make_potentials(oracle, wd, str(tmp_path))
+    rows = []
+    for ws, ps, st, picks in ((w, paths, s, (0, 51)), (wd, dpaths, dense, (3, 200))):
+        oracle.load(w.types, ps, angular=angular)
+        _, centres, nb = oracle.neighbors(st.cell, st.positions, st.types)
+        for i in picks:
+            nbcoo, _, nbl, nbt = nb[i]
+            rows.append((ps, centres[i], int(st.types[i]), nbcoo, nbt))
+    for m in (600, 1, 0):
+        c = np.array([0.3, -0.2, 0.1])
+        d = rng.normal(size=(m, 3))
+        d *= (6.6 * rng.random(m) ** (1 / 3) / np.linalg.norm(d, axis=1))[:, None]
+        rows.append((dpaths, c, 1 + (m % 2), c + d, 1 + rng.integers(0, 2, m)))
+    assert max(len(r[4]) for r in rows[2:4]) > 300
+    ann = None
+    try:
+        for ps, coo_i, ti, coo_j, tj in rows:
+            if ann is None or ann.potential_files != {t: ps[t] for t in w.types}:
+                if ann is not None:
+                    ann.release()
+                ann = _ann(ps, w.types, angular)
+                oracle.load(w.types, ps, angular=angular)
+            m = len(tj)
+            n = m + 1
+            idx = np.arange(2, m + 2, dtype=np.int32)
+            sym = [w.types[t - 1] for t in tj]
+            Fo = np.zeros((n, 3))
+            eo = oracle.atomic_energy_and_forces(coo_i, ti, 1, coo_j, tj, idx, Fo)
+            res = {}
+            for path in ("fused", "graph"):
+                set_option("per_atom_kernel", path)
+                F = np.zeros((n, 3))
+                e = ann.atomic_energy_and_forces(coo_i, w.types[ti - 1], 1, coo_j, sym, idx, F)
+                e2 = ann.atomic_energy(coo_i, w.types[ti - 1], coo_j, sym)
+                F3 = np.zeros((n, 3))
+                e3 = ann.atomic_energy_and_forces(coo_i, w.types[ti - 1], 1, coo_j, sym, idx, F3)
+                assert abs(e - eo) < E_TOL_FP64, (path, m, e, eo)
+                assert np.abs(F - Fo).max() < F_TOL_FP64, (path, m)
+                assert abs(e2 - e) < E_TOL_FP64
+                assert e3 == e and np.array_equal(F3, F)
+                res[path] = (e, F)
+            assert abs(res["fused"][0] - res["graph"][0]) < E_TOL_FP64
+            assert np.abs(res["fused"][1] - res["graph"][1]).max() < F_TOL_FP64
+            if m >= 300 and angular == "current":
+                # the dense rows exercise real forces (the dense potential is
+                # normalised on current-domain descriptors)
+                assert np.abs(Fo).max() > 1e-2
+    finally:
+        set_option("per_atom_kernel", "fused")
+        if ann is not None:
+            ann.release()
+
+
 def test_per_atom_calls_reuse_their_buffers(cuda, oracle, cu256):
     """Repeated aenet_atomic_energy_and_forces calls (the predict.x calling
     pattern) give identical results call after call and across neighbour
