@@ -25,6 +25,10 @@
 //                  32 units are flattened into one candidate index space
 //                  processed 32 candidates at a time; accepted neighbours are
 //                  compacted with ballots into the atom's ELL row.
+//   k_neighbors_struct  one block per structure for batches of small
+//                  structures: wrap and bin, cell counts, scan and scatter
+//                  in shared memory, then the same per-atom search (the
+//                  global cell lists and the kernels above are skipped).
 #include "common.h"
 
 namespace {
@@ -49,11 +53,12 @@ __device__ __forceinline__ double wrap_coordinate(double s, unsigned* status) {
   return w;
 }
 
-__global__ void k_wrap_bin(int natoms, const double* __restrict__ pos,
-                           const int* __restrict__ types, NbBuffers nb) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= natoms) return;
-  const StructGeom* g = nb.geom + nb.atom_struct[i];
+// Lattice coordinates of atom i (geometry.f90:697-712), wrapped, the
+// Cartesian position of the wrapped coordinates and the atom's cell: the
+// per-atom arrays s_wrap, r_wrap, r_f32 (species in w) and cell_of are
+// written; returns the cell's index inside its structure.
+__device__ __forceinline__ int wrap_bin_atom(int i, const StructGeom* g, const double* __restrict__ pos,
+                                             const int* __restrict__ types, const NbBuffers& nb) {
   double r[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
   double s[3], rw[3];
   const int nc[3] = {g->nc[0], g->nc[1], g->nc[2]};
@@ -92,8 +97,6 @@ __global__ void k_wrap_bin(int natoms, const double* __restrict__ pos,
     double x = floor(s[v] * (double)nc[v]);
     cc[v] = x < 0.0 ? 0 : (x >= (double)(nc[v] - 1) ? nc[v] - 1 : (int)x);
   }
-  const int lin = (cc[0] * nc[1] + cc[1]) * nc[2] + cc[2];
-  nb.slot_of[i] = atomicAdd(&nb.cell_count[g->cell_off + lin], 1);
   const int t = types[i];
   for (int v = 0; v < 3; ++v) {
     nb.s_wrap[3 * i + v] = s[v];
@@ -101,6 +104,17 @@ __global__ void k_wrap_bin(int natoms, const double* __restrict__ pos,
   }
   nb.r_f32[i] = make_float4((float)rw[0], (float)rw[1], (float)rw[2], __int_as_float(t));
   nb.cell_of[i] = cc[0] | (cc[1] << 10) | (cc[2] << 20);
+  return (cc[0] * nc[1] + cc[1]) * nc[2] + cc[2];
+}
+
+// one thread per atom; the rank inside the cell from an atomic count
+__global__ void k_wrap_bin(int natoms, const double* __restrict__ pos,
+                           const int* __restrict__ types, NbBuffers nb) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  const StructGeom* g = nb.geom + nb.atom_struct[i];
+  const int lin = wrap_bin_atom(i, g, pos, types, nb);
+  nb.slot_of[i] = atomicAdd(&nb.cell_count[g->cell_off + lin], 1);
 }
 
 // ---- exclusive scan of the cell counts (three phases, 1024 per block)
@@ -492,15 +506,21 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
 }
 
 // One block per structure (structures in the order nb.struct_order, largest
-// first): the structure's cell-ordered positions, atom indices and cell
-// offsets are staged in shared memory, then the block's warps take its
-// atoms one by one with the same search.
+// first), its cell lists built in shared memory: the structure's atoms are
+// wrapped and binned (wrap_bin_atom), counted per cell with shared-memory
+// atomics, the counts scanned and the atoms scattered into cell order
+// (positions, atom indices and cell offsets of the structure only), then
+// the block's warps take its atoms one by one with the same search.  The
+// global cell lists are not used.
 template <typename T4>
-__global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS) k_neighbors_struct(NbBuffers nb) {
+__global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS)
+    k_neighbors_struct(const double* __restrict__ pos, const int* __restrict__ types,
+                       NbBuffers nb) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   __shared__ int su_base[8][32 * NB_UPL];
   __shared__ float4 su_sh[8][32 * NB_UPL];
   __shared__ int su_first[8][32];
+  __shared__ int s_wt[9];
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const StructGeom* g = nb.geom + nb.struct_order[blockIdx.x];
@@ -508,14 +528,47 @@ __global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS) k_neighbors_struct(NbBu
   const int ncell = g->nc[0] * g->nc[1] * g->nc[2];
   float4* spos = reinterpret_cast<float4*>(sm_raw);
   int* satoms = reinterpret_cast<int*>(spos + nb.smem_atoms);
-  int* scs = satoms + nb.smem_atoms;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    spos[q] = nb.cell_pos[a0 + q];
-    satoms[q] = nb.cell_atoms[a0 + q];
-  }
-  for (int q = threadIdx.x; q <= ncell; q += blockDim.x) scs[q] = nb.cell_start[g->cell_off + q];
+  int* scs = satoms + nb.smem_atoms;      // [ncell + 1]: counts, then offsets
+  int* sbin = scs + nb.smem_cells + 1;    // per atom: cell | rank << 16
+  for (int q = threadIdx.x; q <= ncell; q += blockDim.x) scs[q] = 0;
   __syncthreads();
-  const CellSrc src{scs, spos, satoms, a0};
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int lin = wrap_bin_atom(a0 + q, g, pos, types, nb);
+    sbin[q] = lin | (atomicAdd(&scs[lin], 1) << 16);
+  }
+  __syncthreads();
+  // exclusive scan of the counts, 256 at a time
+  int carry = 0;
+  for (int base = 0; base < ncell; base += blockDim.x) {
+    const int c = base + threadIdx.x;
+    const int v = c < ncell ? scs[c] : 0;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += u;
+    }
+    if (lane == 31) s_wt[warp] = incl;
+    __syncthreads();
+    int before = carry, total = 0;
+    for (int w = 0; w < 8; ++w) {
+      if (w < warp) before += s_wt[w];
+      total += s_wt[w];
+    }
+    if (c < ncell) scs[c] = before + incl - v;
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) scs[ncell] = n;
+  __syncthreads();
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int w = sbin[q];
+    const int p = scs[w & 0xffff] + (w >> 16);
+    spos[p] = nb.r_f32[a0 + q];
+    satoms[p] = a0 + q;
+  }
+  __syncthreads();
+  const CellSrc src{scs, spos, satoms, 0};
   for (int a = warp; a < n; a += (blockDim.x >> 5))
     search_atom<T4>(a0 + a, nb, g, src, su_base[warp], su_sh[warp], su_first[warp], lane);
 }
@@ -1285,6 +1338,23 @@ int ae_launch_ell_from_csr(int nlocal, int nall, const double* x, const int* typ
 int ae_launch_neighbors(int natoms, const double* pos, const int* types, const NbBuffers& nb,
                         int fp64, cudaStream_t s) {
   if (natoms <= 0) return 0;
+  if (nb.cell_kernel == 4 && nb.struct_order) {
+    // cell lists built inside the search blocks
+    if (nb.ev_search) cudaEventRecord(nb.ev_search, s);
+    const size_t smem = 24 * (size_t)nb.smem_atoms + 4 * ((size_t)nb.smem_cells + 1);
+    if (fp64) {
+      auto kern = k_neighbors_struct<double4_32a>;
+      if (smem + 24576 > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<nb.nstruc, 256, smem, s>>>(pos, types, nb);
+    } else {
+      auto kern = k_neighbors_struct<float4>;
+      if (smem + 24576 > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<nb.nstruc, 256, smem, s>>>(pos, types, nb);
+    }
+    return (int)cudaGetLastError();
+  }
   const int nc = nb.ncells_total;
   cudaError_t e = cudaMemsetAsync(nb.cell_count, 0, sizeof(int) * (size_t)nc, s);
   if (e != cudaSuccess) return (int)e;
@@ -1296,21 +1366,6 @@ int ae_launch_neighbors(int natoms, const double* pos, const int* types, const N
   k_scan_add<<<nblk, SCAN_B, 0, s>>>(nc, nb.cell_start, nb.scan_tmp);
   k_scatter<<<(natoms + 255) / 256, 256, 0, s>>>(natoms, nb);
   if (nb.ev_search) cudaEventRecord(nb.ev_search, s);
-  if (nb.cell_kernel == 4 && nb.struct_order) {
-    const size_t smem = 20 * (size_t)nb.smem_atoms + 4 * ((size_t)nb.smem_cells + 1);
-    if (fp64) {
-      auto kern = k_neighbors_struct<double4_32a>;
-      if (smem + 24576 > 48 * 1024)
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      kern<<<nb.nstruc, 256, smem, s>>>(nb);
-    } else {
-      auto kern = k_neighbors_struct<float4>;
-      if (smem + 24576 > 48 * 1024)
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      kern<<<nb.nstruc, 256, smem, s>>>(nb);
-    }
-    return (int)cudaGetLastError();
-  }
   if (nb.cell_kernel == 3) {
     e = cudaMemsetAsync(nb.nb_cnt, 0, sizeof(int) * (size_t)natoms, s);
     if (e != cudaSuccess) return (int)e;
