@@ -23,7 +23,7 @@ from .plan import Plan
 LANES = (8, 16, 32)
 CELL_DIVS = (1, 2, 3)
 Z_REFINES = (1, 2, 4)
-NB_KERNELS = ("cell", "atom", "stream", "half", "struct")
+NB_KERNELS = ("cell", "atom", "stream", "half", "struct", "struct_half")
 CACHE = os.path.join(os.path.expanduser("~"), ".cache", "aenet_gb300", "autotune.json")
 
 

@@ -1214,8 +1214,8 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   size_t o_ord = take(4 * (size_t)N);
   size_t o_spo = take(4 * (AE_MAXT + 1));
   size_t o_ps = take(4 * (size_t)ae_part_scratch_ints(N));
-  // per-structure search: every structure's cell lists (24 B per atom, 4 B
-  // per cell) fit one block's shared memory (at most 48 KB with the unit
+  // per-structure search: every structure's cell lists and row counters
+  // (28 B per atom, 4 B per cell) fit one block's shared memory (at most 48 KB with the unit
   // tables)
   int max_n = 0, max_c = 0;
   for (int s = 0; s < P->nstruc; ++s) {
@@ -1229,7 +1229,7 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     nsm = 0;
   const bool per_struct = nsm > 0 && P->nstruc >= 2 * nsm &&
-                          24 * (size_t)max_n + 4 * ((size_t)max_c + 1) + 24576 <= 48 * 1024;
+                          28 * (size_t)max_n + 4 * ((size_t)max_c + 1) + 24576 <= 48 * 1024;
   size_t o_so2 = per_struct ? take(4 * (size_t)P->nstruc) : 0;
   if (cudaMalloc(&P->mem, off) != cudaSuccess) return AENET_ERR_CUDA;
   P->mem_bytes = off;
@@ -2270,6 +2270,7 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     else if (v == "stream") g.nb_cell = 2;
     else if (v == "half") g.nb_cell = 3;
     else if (v == "struct") g.nb_cell = 4;
+    else if (v == "struct_half") g.nb_cell = 5;
     else if (v == "atom") g.nb_cell = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;

@@ -505,6 +505,58 @@ __global__ void __launch_bounds__(256, 4) k_neighbors(int natoms, NbBuffers nb) 
   search_atom<T4>(i, nb, g, src, su_base[warp], su_sh[warp], su_first[warp], lane);
 }
 
+// The cell lists of one structure in shared memory (block-wide): atoms
+// wrapped and binned (wrap_bin_atom), counted per cell with shared-memory
+// atomics, the counts scanned (scs[c] = first entry of cell c, scs[ncell] =
+// n) and the atoms scattered into cell order (spos, satoms).
+__device__ __forceinline__ void struct_cells(const StructGeom* g, const double* __restrict__ pos,
+                                             const int* __restrict__ types, const NbBuffers& nb,
+                                             float4* spos, int* satoms, int* scs, int* sbin,
+                                             int* s_wt) {
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int n = g->natoms, a0 = g->atom_off;
+  const int ncell = g->nc[0] * g->nc[1] * g->nc[2];
+  for (int q = threadIdx.x; q <= ncell; q += blockDim.x) scs[q] = 0;
+  __syncthreads();
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int lin = wrap_bin_atom(a0 + q, g, pos, types, nb);
+    sbin[q] = lin | (atomicAdd(&scs[lin], 1) << 16);
+  }
+  __syncthreads();
+  // exclusive scan of the counts, a block's width at a time
+  int carry = 0;
+  for (int base = 0; base < ncell; base += blockDim.x) {
+    const int c = base + threadIdx.x;
+    const int v = c < ncell ? scs[c] : 0;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += u;
+    }
+    if (lane == 31) s_wt[warp] = incl;
+    __syncthreads();
+    int before = carry, total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      if (w < warp) before += s_wt[w];
+      total += s_wt[w];
+    }
+    if (c < ncell) scs[c] = before + incl - v;
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) scs[ncell] = n;
+  __syncthreads();
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int w = sbin[q];
+    const int p = scs[w & 0xffff] + (w >> 16);
+    spos[p] = nb.r_f32[a0 + q];
+    satoms[p] = a0 + q;
+  }
+  __syncthreads();
+}
+
 // One block per structure (structures in the order nb.struct_order, largest
 // first), its cell lists built in shared memory: the structure's atoms are
 // wrapped and binned (wrap_bin_atom), counted per cell with shared-memory
@@ -525,49 +577,11 @@ __global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS)
   const int lane = threadIdx.x & 31;
   const StructGeom* g = nb.geom + nb.struct_order[blockIdx.x];
   const int n = g->natoms, a0 = g->atom_off;
-  const int ncell = g->nc[0] * g->nc[1] * g->nc[2];
   float4* spos = reinterpret_cast<float4*>(sm_raw);
   int* satoms = reinterpret_cast<int*>(spos + nb.smem_atoms);
   int* scs = satoms + nb.smem_atoms;      // [ncell + 1]: counts, then offsets
   int* sbin = scs + nb.smem_cells + 1;    // per atom: cell | rank << 16
-  for (int q = threadIdx.x; q <= ncell; q += blockDim.x) scs[q] = 0;
-  __syncthreads();
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int lin = wrap_bin_atom(a0 + q, g, pos, types, nb);
-    sbin[q] = lin | (atomicAdd(&scs[lin], 1) << 16);
-  }
-  __syncthreads();
-  // exclusive scan of the counts, 256 at a time
-  int carry = 0;
-  for (int base = 0; base < ncell; base += blockDim.x) {
-    const int c = base + threadIdx.x;
-    const int v = c < ncell ? scs[c] : 0;
-    int incl = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int u = __shfl_up_sync(0xffffffffu, incl, d);
-      if (lane >= d) incl += u;
-    }
-    if (lane == 31) s_wt[warp] = incl;
-    __syncthreads();
-    int before = carry, total = 0;
-    for (int w = 0; w < 8; ++w) {
-      if (w < warp) before += s_wt[w];
-      total += s_wt[w];
-    }
-    if (c < ncell) scs[c] = before + incl - v;
-    carry += total;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) scs[ncell] = n;
-  __syncthreads();
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int w = sbin[q];
-    const int p = scs[w & 0xffff] + (w >> 16);
-    spos[p] = nb.r_f32[a0 + q];
-    satoms[p] = a0 + q;
-  }
-  __syncthreads();
+  struct_cells(g, pos, types, nb, spos, satoms, scs, sbin, s_wt);
   const CellSrc src{scs, spos, satoms, 0};
   for (int a = warp; a < n; a += (blockDim.x >> 5))
     search_atom<T4>(a0 + a, nb, g, src, su_base[warp], su_sh[warp], su_first[warp], lane);
@@ -1249,6 +1263,236 @@ __global__ void __launch_bounds__(256, 4) k_neighbors_half(int natoms, NbBuffers
   }
 }
 
+// ---- half stencil per structure: the shared-memory cell lists of
+// k_neighbors_struct walked as k_neighbors_half walks the global ones (each
+// unordered pair met once and written to both rows), the rows' counters in
+// shared memory.  Same sets as the full search; the order inside a row
+// depends on timing.
+template <typename T4>
+__device__ __forceinline__ void search_atom_half(int i, int a0, const NbBuffers& nb,
+                                                 const StructGeom* g, const float4* spos,
+                                                 const int* satoms, const int* scs, int* scnt,
+                                                 int* su_base_w, float4* su_sh_w,
+                                                 int* su_first_w, int lane) {
+  const int pbc = g->pbc;
+  const int nc0 = g->nc[0], nc1 = g->nc[1], nc2 = g->nc[2];
+  const int k0 = g->kr[0], k1 = g->kr[1], k2 = g->kr[2];
+  const int w1 = 2 * k1 + 1;
+  const int packed = nb.cell_of[i];
+  const int c0 = packed & 1023, c1 = (packed >> 10) & 1023, c2 = (packed >> 20) & 1023;
+  const int t2lo = pbc ? floor_div_r(c2 - k2, g->inv_nc[2]) : 0;
+  const int t2hi = pbc ? floor_div_r(c2 + k2, g->inv_nc[2]) : 0;
+  const int nt2 = t2hi - t2lo + 1;
+  // rows (0, 0..k1) then (1..k0, -k1..k1); the (0, 0) row from dz = 0 up
+  const int nrows = (k1 + 1) + k0 * w1;
+  const int nunits = nrows * nt2;
+  const float4 ri = nb.r_f32[i];
+  const int iti = i | (__float_as_int(ri.w) << AE_TYPE_SHIFT);
+  const float rc2_lo = g->rc2_lo, rc2_hi = g->rc2_hi;
+  const double rc2 = g->rc2;
+  const int cap = nb.cap;
+  const int* __restrict__ cstart = scs;
+  const int home_end = cstart[(c0 * nc1 + c1) * nc2 + c2 + 1];
+  const float sf0 = (float)nb.s_wrap[3 * i], sf1 = (float)nb.s_wrap[3 * i + 1],
+              sf2 = (float)nb.s_wrap[3 * i + 2];
+  const float rcf = g->rcf * 1.0001f + 1e-4f;
+  const float inv_nt2 = __fdividef(1.0f, (float)nt2), inv_w1 = __fdividef(1.0f, (float)w1);
+  const float inc0 = g->inv_nc[0], inc1 = g->inv_nc[1];
+  const int ortho = g->ortho;
+  const float hf0 = g->hf[0], hf1 = g->hf[1], ihf2 = g->inv_hf[2];
+  const float* __restrict__ Lf = g->Lf;
+  const unsigned lt = (1u << lane) - 1u;
+
+  for (int ubase = 0; ubase < nunits; ubase += 32) {
+    const int u = ubase + lane;
+    int len = 0, beg = 0, T0 = 0, T1 = 0, T2 = 0, home = 0;
+    float sh0 = 0.f, sh1 = 0.f, sh2 = 0.f;
+    if (u < nunits) {
+      const int rr = floor_div_r(u, inv_nt2);
+      const int it2 = u - rr * nt2;
+      int d0, d1;
+      if (rr <= k1) {
+        d0 = 0;
+        d1 = rr;
+      } else {
+        const int r2 = rr - (k1 + 1);
+        const int q0 = floor_div_r(r2, inv_w1);
+        d0 = 1 + q0;
+        d1 = r2 - q0 * w1 - k1;
+      }
+      int a0 = c0 + d0, a1 = c1 + d1;
+      bool ok = true;
+      int zlo = (d0 == 0 && d1 == 0) ? c2 : c2 - k2, zhi = c2 + k2;
+      if (ortho) {
+        const float x0 = (float)a0 * inc0, x1 = (float)(a0 + 1) * inc0;
+        const float y0 = (float)a1 * inc1, y1 = (float)(a1 + 1) * inc1;
+        const float gx = fmaxf(0.f, fmaxf(x0 - sf0, sf0 - x1)) * hf0;
+        const float gy = fmaxf(0.f, fmaxf(y0 - sf1, sf1 - y1)) * hf1;
+        const float rem = rcf * rcf - gx * gx - gy * gy;
+        if (rem < 0.f) {
+          ok = false;
+        } else {
+          const float hz = sqrtf(rem) * ihf2 * 1.0001f + 1e-6f;
+          zlo = max(zlo, (int)floorf((sf2 - hz) * nc2));
+          zhi = min(zhi, (int)floorf((sf2 + hz) * nc2));
+        }
+      }
+      if (pbc) {
+        T0 = floor_div_r(a0, inc0);
+        a0 -= T0 * nc0;
+        T1 = floor_div_r(a1, inc1);
+        a1 -= T1 * nc1;
+        T2 = t2lo + it2;
+        zlo = max(zlo, T2 * nc2);
+        zhi = min(zhi, T2 * nc2 + nc2 - 1);
+      } else {
+        ok = ok && it2 == 0 && a0 >= 0 && a0 < nc0 && a1 >= 0 && a1 < nc1;
+        zlo = max(zlo, 0);
+        zhi = min(zhi, nc2 - 1);
+      }
+      if (ok && zlo <= zhi) {
+        const int base = (a0 * nc1 + a1) * nc2 - T2 * nc2;
+        beg = cstart[base + zlo];
+        len = cstart[base + zhi + 1] - beg;
+        // the home cell (T = 0) leads the (0, 0) row of image 0
+        home = (d0 == 0 && d1 == 0 && zlo == c2) ? AE_HOME_UNIT : 0;
+        const float f0 = (float)T0, f1 = (float)T1, f2 = (float)T2;
+        sh0 = f0 * Lf[0] + f1 * Lf[3] + f2 * Lf[6];
+        sh1 = f0 * Lf[1] + f1 * Lf[4] + f2 * Lf[7];
+        sh2 = f0 * Lf[2] + f1 * Lf[5] + f2 * Lf[8];
+      }
+    }
+    int incl = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int w = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += w;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int start = incl - len;
+    __syncwarp();
+    su_base_w[lane] = beg - start;
+    su_sh_w[lane] = make_float4(
+        sh0, sh1, sh2,
+        __int_as_float((T0 & 1023) | ((T1 & 1023) << 10) | ((T2 & 1023) << 20) | home));
+    __syncwarp();
+    int carry = 0;
+    for (int qb = 0; qb < total; qb += 32) {
+      const int q = qb + lane;
+      const bool starts = len > 0 && start >= qb && start < qb + 32;
+      __syncwarp();
+      if (starts) su_first_w[start - qb] = lane;
+      const unsigned marks = __reduce_or_sync(0xffffffffu, starts ? (1u << (start - qb)) : 0u);
+      __syncwarp();
+      const unsigned upto = marks & (0xffffffffu >> (31 - lane));
+      const int own = upto ? su_first_w[31 - __clz(upto)] : carry;
+      carry = __shfl_sync(0xffffffffu, own, 31);
+      const float4 osh = su_sh_w[own];
+      const int tag = __float_as_int(osh.w);
+      const int img = tag & ~AE_HOME_UNIT;
+      bool acc_i = false, acc_j = false;
+      int j = 0, tj = 0;
+      float dx = 0.f, dy = 0.f, dz = 0.f, dd2 = 0.f;
+      if (q < total) {
+        const int p = su_base_w[own] + q;
+        const float4 rj = spos[p];
+        j = satoms[p];
+        tj = __float_as_int(rj.w);
+        // in the atom's own cell only partners after it
+        if (!(tag & AE_HOME_UNIT) || p >= home_end || j > i) {
+          dx = (rj.x - ri.x) + osh.x;
+          dy = (rj.y - ri.y) + osh.y;
+          dz = (rj.z - ri.z) + osh.z;
+          dd2 = dx * dx + dy * dy + dz * dz;
+          if (dd2 < rc2_lo) {
+            acc_i = acc_j = true;
+          } else if (dd2 <= rc2_hi) {
+            const int t0 = sext10i(img & 1023), t1 = sext10i((img >> 10) & 1023),
+                      t2 = sext10i((img >> 20) & 1023);
+            acc_i = band_accept(g, nb, pbc, i, j, t0, t1, t2, rc2);
+            acc_j = band_accept(g, nb, pbc, j, i, -t0, -t1, -t2, rc2);
+          }
+        }
+      }
+      // row i: one counter update per batch
+      const unsigned mask = __ballot_sync(0xffffffffu, acc_i);
+      int base_i = 0;
+      if (mask) {
+        if (lane == 0) base_i = atomicAdd(scnt + (i - a0), __popc(mask));
+        base_i = __shfl_sync(0xffffffffu, base_i, 0);
+      }
+      const int nimg = ((-sext10i(img & 1023)) & 1023) |
+                       (((-sext10i((img >> 10) & 1023)) & 1023) << 10) |
+                       (((-sext10i((img >> 20) & 1023)) & 1023) << 20);
+      if (acc_i) {
+        const int k = base_i + __popc(mask & lt);
+        if (k < cap) {
+          const size_t row = (size_t)i * cap;
+          nb.nb_jt[row + k] = j | (tj << AE_TYPE_SHIFT);
+          if (nb.nb_img) nb.nb_img[row + k] = img;
+          if (VecOut<T4>::fp64) {
+            reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] = fp64_pair_vector(
+                g, nb, pbc, i, j, sext10i(img & 1023), sext10i((img >> 10) & 1023),
+                sext10i((img >> 20) & 1023));
+          } else {
+            reinterpret_cast<float4*>(nb.nb_vec)[row + k] =
+                make_float4(dx, dy, dz, pair_length(dd2));
+          }
+        }
+      }
+      // row j: the mirrored pair
+      if (acc_j) {
+        const int k = atomicAdd(scnt + (j - a0), 1);
+        if (k < cap) {
+          const size_t row = (size_t)j * cap;
+          nb.nb_jt[row + k] = iti;
+          if (nb.nb_img) nb.nb_img[row + k] = nimg;
+          if (VecOut<T4>::fp64) {
+            reinterpret_cast<double4_32a*>(nb.nb_vec)[row + k] = fp64_pair_vector(
+                g, nb, pbc, j, i, -sext10i(img & 1023), -sext10i((img >> 10) & 1023),
+                -sext10i((img >> 20) & 1023));
+          } else {
+            reinterpret_cast<float4*>(nb.nb_vec)[row + k] =
+                make_float4(-dx, -dy, -dz, pair_length(dd2));
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename T4>
+__global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS)
+    k_neighbors_struct_half(const double* __restrict__ pos, const int* __restrict__ types,
+                            NbBuffers nb) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  __shared__ int su_base[8][32];
+  __shared__ float4 su_sh[8][32];
+  __shared__ int su_first[8][32];
+  __shared__ int s_wt[9];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const StructGeom* g = nb.geom + nb.struct_order[blockIdx.x];
+  const int n = g->natoms, a0 = g->atom_off;
+  float4* spos = reinterpret_cast<float4*>(sm_raw);
+  int* satoms = reinterpret_cast<int*>(spos + nb.smem_atoms);
+  int* scs = satoms + nb.smem_atoms;
+  int* sbin = scs + nb.smem_cells + 1;
+  int* scnt = sbin + nb.smem_atoms;       // row counters
+  for (int q = threadIdx.x; q < n; q += blockDim.x) scnt[q] = 0;
+  struct_cells(g, pos, types, nb, spos, satoms, scs, sbin, s_wt);
+  for (int a = warp; a < n; a += (blockDim.x >> 5))
+    search_atom_half<T4>(a0 + a, a0, nb, g, spos, satoms, scs, scnt, su_base[warp], su_sh[warp],
+                         su_first[warp], lane);
+  __syncthreads();
+  const int cap = nb.cap;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int c = scnt[q];
+    nb.nb_cnt[a0 + q] = min(c, cap);
+    if (c > cap) atomicOr(nb.status, AE_ST_NB_OVERFLOW);
+  }
+}
+
 // counts of the half-stencil search: clamp to the capacity, flag overflow
 __global__ void k_clamp_counts(int natoms, int cap, int* __restrict__ cnt, unsigned* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1338,6 +1582,23 @@ int ae_launch_ell_from_csr(int nlocal, int nall, const double* x, const int* typ
 int ae_launch_neighbors(int natoms, const double* pos, const int* types, const NbBuffers& nb,
                         int fp64, cudaStream_t s) {
   if (natoms <= 0) return 0;
+  if (nb.cell_kernel == 5 && nb.struct_order) {
+    // half stencil, cell lists and row counters inside the search blocks
+    if (nb.ev_search) cudaEventRecord(nb.ev_search, s);
+    const size_t smem = 28 * (size_t)nb.smem_atoms + 4 * ((size_t)nb.smem_cells + 1);
+    if (fp64) {
+      auto kern = k_neighbors_struct_half<double4_32a>;
+      if (smem + 24576 > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<nb.nstruc, 256, smem, s>>>(pos, types, nb);
+    } else {
+      auto kern = k_neighbors_struct_half<float4>;
+      if (smem + 24576 > 48 * 1024)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<nb.nstruc, 256, smem, s>>>(pos, types, nb);
+    }
+    return (int)cudaGetLastError();
+  }
   if (nb.cell_kernel == 4 && nb.struct_order) {
     // cell lists built inside the search blocks
     if (nb.ev_search) cudaEventRecord(nb.ev_search, s);

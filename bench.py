@@ -61,7 +61,7 @@ def parse():
                     help="fix the descriptor kernels' lanes per atom (implies --no-tune)")
     ap.add_argument("--cell-div", type=int, default=0,
                     help="fix the neighbour grid's cells per cut-off (implies --no-tune)")
-    ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom", "stream", "half", "struct"],
+    ap.add_argument("--neighbour-kernel", default="", choices=["", "cell", "atom", "stream", "half", "struct", "struct_half"],
                     help="fix the neighbour-search kernel (implies --no-tune)")
     ap.add_argument("--z-refine", type=int, default=0,
                     help="search cells this many times narrower along the third axis")

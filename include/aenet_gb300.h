@@ -48,7 +48,8 @@ extern "C" {
  *       atom (performance only).
  *   "adjoint_lanes_per_atom" = "0" | "8" | "16" | "32"   the same for the
  *       adjoint kernels; 0 follows lanes_per_atom (performance only).
- *   "neighbour_kernel" = "atom" | "cell" | "stream" | "half" | "struct"   neighbour
+ *   "neighbour_kernel" = "atom" | "cell" | "stream" | "half" | "struct" |
+ *       "struct_half"   neighbour
  *       search with one warp per atom (pruned per atom), one warp per home
  *       cell with a lane per home atom (dense cells of large structures),
  *       one warp per home cell with a lane per candidate, each batch of
@@ -56,7 +57,9 @@ extern "C" {
  *       one warp per atom over half the stencil, each pair found once and
  *       written to both rows (the order inside a row then varies from run
  *       to run), or one block per structure with the structure's cell
- *       lists staged in shared memory and warps taking its atoms in turn
+ *       lists built in shared memory and warps taking its atoms in turn,
+ *       over the full stencil (struct) or the half stencil with both rows
+ *       written (struct_half; row order then varies from run to run)
  *       (batches of small structures; plans with fewer structures than
  *       twice the SMs, or whose largest structure does not fit a block,
  *       use the warp-per-atom search); same neighbour sets (performance

@@ -942,11 +942,12 @@ def test_per_atom_calls_reuse_their_buffers(cuda, oracle, cu256):
 
 
 def test_per_structure_search_matches_per_atom_search(cuda, oracle, tmp_path):
-    """The block-per-structure search (taken for batches of more than twice
-    as many structures as SMs) against the warp-per-atom search on 320
-    small cells: identical (neighbour, image) sets per row, in both
-    precisions, on the plain and the refined grid; FP64 energies equal to
-    rounding and against the oracle on a sample of cells."""
+    """The block-per-structure searches, full and half stencil (taken for
+    batches of more than twice as many structures as SMs), against the
+    warp-per-atom search on 320 small cells: identical (neighbour, image)
+    sets per row, in both precisions, on the plain and the refined grid;
+    FP64 energies equal to rounding and against the oracle on a sample of
+    cells."""
     torch = cuda
     from aenet_gb300 import workloads
     from aenet_gb300.core import FP64, MIXED, set_option
@@ -962,18 +963,21 @@ def test_per_structure_search_matches_per_atom_search(cuda, oracle, tmp_path):
             set_option("z_refine", z)
             for prec in (FP64, MIXED):
                 got = {}
-                for kern in ("atom", "struct"):
+                for kern in ("atom", "struct", "struct_half"):
                     set_option("neighbour_kernel", kern)
                     plan = Plan(nat, cells, pbc, precision=prec)
                     o = plan.run(p, t)
                     plan.check()
                     got[kern] = _neighbour_keys(torch, plan, p, cells, nat) + (o["E"].clone(),)
                     plan.close()
-                a, s = got["atom"], got["struct"]
-                assert torch.equal(a[0], s[0])
-                assert torch.equal(a[1], s[1])
+                a = got["atom"]
                 tol = 1e-11 if prec == FP64 else 1e-5
-                assert ((a[4] - s[4]).abs() / torch.as_tensor(nat, device="cuda")).max() < tol
+                for kern in ("struct", "struct_half"):
+                    s = got[kern]
+                    assert torch.equal(a[0], s[0]), kern
+                    assert torch.equal(a[1], s[1]), kern
+                    assert ((a[4] - s[4]).abs() / torch.as_tensor(nat, device="cuda")).max() < tol
+                s = got["struct"]
                 if prec == FP64 and z == 4:
                     E = s[4].cpu().numpy()
         oracle.load(w.types, paths)
