@@ -263,6 +263,11 @@ constexpr int NB_UPL = 1;
 #ifndef NB_STRUCT_BLOCKS
 #define NB_STRUCT_BLOCKS 4
 #endif
+// the half-stencil variant runs faster with three blocks per SM (its
+// registers then hold the search state without spilling)
+#ifndef NB_STRUCT_HALF_BLOCKS
+#define NB_STRUCT_HALF_BLOCKS 3
+#endif
 
 // Where a search reads the cell lists: the global arrays, or one
 // structure's copy in shared memory (cell-ordered entries p at p - base).
@@ -1462,7 +1467,7 @@ __device__ __forceinline__ void search_atom_half(int i, int a0, const NbBuffers&
 }
 
 template <typename T4>
-__global__ void __launch_bounds__(256, NB_STRUCT_BLOCKS)
+__global__ void __launch_bounds__(256, NB_STRUCT_HALF_BLOCKS)
     k_neighbors_struct_half(const double* __restrict__ pos, const int* __restrict__ types,
                             NbBuffers nb) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
