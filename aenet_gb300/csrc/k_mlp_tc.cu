@@ -272,6 +272,19 @@ __global__ void __launch_bounds__(128) k_mlp_tc(PotDevice pd, DescBuffers b,
     const bool valid = m < cnt;
     const int atom = valid ? order[beg + m] : 0;
     const int nsf = pd.sp[t].nsf;
+    // the next tile's atom: its descriptor row is prefetched into L2 once
+    // the first MMA round of this tile has been issued
+    int atom_next = -1;
+    if (q + 1 < q1) {
+      int tn = 0, acn = 0;
+      for (; tn < pd.ntypes; ++tn) {
+        const int tt = (spec_off[tn + 1] - spec_off[tn] + TILE - 1) / TILE;
+        if (q + 1 < acn + tt) break;
+        acn += tt;
+      }
+      const int bn = spec_off[tn] + (q + 1 - acn) * TILE;
+      if (m < min(TILE, spec_off[tn + 1] - bn)) atom_next = order[bn + m];
+    }
 
     // ---- descriptor row -> A operand
     {
@@ -295,6 +308,12 @@ __global__ void __launch_bounds__(128) k_mlp_tc(PotDevice pd, DescBuffers b,
     if (m == 0) {
       gemm_split<KIN, H>(tmem, sAh, sAl, sImg + L.b1, sImg + L.b1 + 2 * H * KIN);
       mma_commit(mb);
+    }
+    if (atom_next >= 0) {
+      const float* Gn = reinterpret_cast<const float*>(b.G) + (size_t)atom_next * pd.nsf_pad;
+#pragma unroll
+      for (int k = 0; k < KIN; k += 32)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(Gn + k)));
     }
     ok = __syncthreads_and(mbar_wait(mb, phase));
     phase ^= 1u;
