@@ -275,8 +275,10 @@ struct State {
                              // warp per atom over the half stencil (3)
   int angular_moments = 1;   // FP32 angular terms in moment form where instantiated
   int angular_spin_stale = 0;  // Chebyshev spin block with sfb_eval's stale s_j
-  int atom_fused = 1;          // per-atom calls: one fused launch (1) or the graph of the
-                               // batch kernels (0)
+  int atom_fused = 2;          // per-atom calls: one fused launch, on a cluster of blocks for
+                               // rows of AE_ATOM_CLUSTER_ROWS neighbours or more and on one
+                               // block below (2), always on a cluster (3), always on one
+                               // block (1); or the graph of the batch kernels (0)
   std::vector<double> scale_host;   // 1/s per [type][nsf_pad] of the loaded tables
   // device tables
   bool dev_ready = false;
@@ -1665,9 +1667,10 @@ int atom_mapped_reserve(size_t bytes) {
   return 0;
 }
 
-// One FP64 Chebyshev atom in one launch of the fused per-atom kernel, the
-// row and the results in mapped host memory; AE_ATOM_NA when the potential
-// or the row does not fit that kernel.
+// One FP64 Chebyshev atom in one launch of the fused per-atom kernel (a
+// cluster of blocks, or one block), the row and the results in mapped host
+// memory; AE_ATOM_NA when the potential or the row does not fit that
+// kernel.
 int atomic_eval_fused(const double* coo_i, int type_i, int n_j, const double* coo_j,
                       const int* type_j, double* E_i, double* F_local) {
   const size_t in_bytes =
@@ -1694,7 +1697,11 @@ int atomic_eval_fused(const double* coo_i, int type_i, int n_j, const double* co
     ty[j] = type_j[j] - 1;
   }
   const char* ho = h + in_bytes;
-  const int e = ae_launch_atom(g.pd, n_j, g_atom.mdev, g_atom.mdev + in_bytes, g_atom.stream);
+  // one block is faster for short rows (a cluster's launch and barriers
+  // cost a few microseconds), the cluster for long ones
+  const bool cluster = g.atom_fused == 3 || (g.atom_fused == 2 && n_j >= AE_ATOM_CLUSTER_ROWS);
+  const int e = ae_launch_atom(g.pd, n_j, g_atom.mdev, g_atom.mdev + in_bytes, cluster,
+                               g_atom.stream);
   if (e == AE_ATOM_NA) return AE_ATOM_NA;
   if (e || cudaStreamSynchronize(g_atom.stream) != cudaSuccess) return AENET_ERR_CUDA;
   if (*reinterpret_cast<const unsigned*>(ho + 8)) return AENET_ERR_CUDA;
@@ -2282,7 +2289,9 @@ EXPORT int aenet_gpu_set_option(const char* key, const char* value) {
     return AENET_OK;
   }
   if (k == "per_atom_kernel") {
-    if (v == "fused") g.atom_fused = 1;
+    if (v == "fused") g.atom_fused = 2;
+    else if (v == "cluster") g.atom_fused = 3;
+    else if (v == "block") g.atom_fused = 1;
     else if (v == "graph") g.atom_fused = 0;
     else return AENET_ERR_INPUT;
     return AENET_OK;

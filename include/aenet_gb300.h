@@ -85,11 +85,14 @@ extern "C" {
  *       Pair form only (the moment form is skipped); applies to plans
  *       created afterwards; the force term of the training loss and the
  *       descriptor Jacobians need "own" (AENET_ERR_INPUT otherwise).
- *   "per_atom_kernel" = "fused" | "graph"   aenet_atomic_energy(_and_forces)
- *       on Chebyshev potentials (orders up to 24 radial, 16 angular; up to
- *       512 neighbours; angular_spin own): one block evaluates the call in
- *       one launch, the row read from and the results written to mapped
- *       host memory (fused), or the batch kernels run on a one-row table
+ *   "per_atom_kernel" = "fused" | "cluster" | "block" | "graph"
+ *       aenet_atomic_energy(_and_forces) on Chebyshev potentials (orders up
+ *       to 24 radial, 16 angular; up to 512 neighbours; angular_spin own):
+ *       one launch evaluates the call, the row read from and the results
+ *       written to mapped host memory, on a cluster of eight blocks that
+ *       split the rows and pairs (cluster), on one block (block), or on
+ *       one block for rows under 96 neighbours and a cluster from there
+ *       (fused, the default); or the batch kernels run on a one-row table
  *       from a captured graph (graph; also what Behler potentials, stale
  *       spins and longer rows always take).  Same results to FP64
  *       rounding.

@@ -831,9 +831,9 @@ def test_stale_spin_option_matches_oracle(cuda, oracle, tmp_path):
 @pytest.mark.parametrize("angular", ["current", "legacy"])
 def test_fused_per_atom_kernel_matches_oracle_and_graph_path(cuda, oracle, aucu, angular,
                                                               tmp_path):
-    """The fused per-atom launch (one block per call, FP64) against the
-    oracle and against the graph of the batch kernels (per_atom_kernel =
-    graph): two species with the spin block, both angular domains, rows of
+    """The fused per-atom launch (FP64; a cluster of eight blocks, and one
+    block) against the oracle and against the graph of the batch kernels
+    (per_atom_kernel = cluster, block, graph): two species with the spin block, both angular domains, rows of
     the alloy cell (about 80 neighbours, 24 angular), rows of a dense
     random cell (over 300 neighbours, about 110 angular: several staging
     chunks and pair rounds), a row beyond the fused kernel's 512
@@ -888,7 +888,7 @@ def test_fused_per_atom_kernel_matches_oracle_and_graph_path(cuda, oracle, aucu,
             Fo = np.zeros((n, 3))
             eo = oracle.atomic_energy_and_forces(coo_i, ti, 1, coo_j, tj, idx, Fo)
             res = {}
-            for path in ("fused", "graph"):
+            for path in ("cluster", "block", "graph"):
                 set_option("per_atom_kernel", path)
                 F = np.zeros((n, 3))
                 e = ann.atomic_energy_and_forces(coo_i, w.types[ti - 1], 1, coo_j, sym, idx, F)
@@ -900,8 +900,9 @@ def test_fused_per_atom_kernel_matches_oracle_and_graph_path(cuda, oracle, aucu,
                 assert abs(e2 - e) < E_TOL_FP64
                 assert e3 == e and np.array_equal(F3, F)
                 res[path] = (e, F)
-            assert abs(res["fused"][0] - res["graph"][0]) < E_TOL_FP64
-            assert np.abs(res["fused"][1] - res["graph"][1]).max() < F_TOL_FP64
+            for path in ("cluster", "block"):
+                assert abs(res[path][0] - res["graph"][0]) < E_TOL_FP64
+                assert np.abs(res[path][1] - res["graph"][1]).max() < F_TOL_FP64
             if m >= 300 and angular == "current":
                 # the dense rows exercise real forces (the dense potential is
                 # normalised on current-domain descriptors)
