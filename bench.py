@@ -385,7 +385,7 @@ def run_gb300(args):
     if os.path.exists(tf):
         traffic_per_atom = json.load(open(tf))
     limiters = {}
-    lf = os.path.join(ROOT, "profiles", "limiters_lisio_batch_512.txt")
+    lf = os.path.join(ROOT, "profiles", "limiters_lisio_batch_1024.txt")
     if os.path.exists(lf):
         limiters = json.load(open(lf))
     times = {"k_neighbors": stages["neighbour_search"], "k_cheb_forward": stages["descriptor"],
@@ -413,7 +413,7 @@ def run_gb300(args):
         if tpa is not None and alg:
             r["traffic_over_algorithmic"] = tpa * N / alg
         if limiters.get(k):
-            r["limiter"] = dict(limiters[k], source="profiles/ncu_full_lisio_batch_512.md")
+            r["limiter"] = dict(limiters[k], source="profiles/ncu_full_lisio_batch_1024.md")
         kernels_roof[k] = r
     dom = max(times, key=lambda k: times[k])
     roof = dict(kernels_roof[dom], kernel=dom)
@@ -611,9 +611,16 @@ def run_gb300(args):
     if rank == 0 and not args.no_md:
         md = run_md(args, local)
 
-    launches_per_step = 16   # types, 6 neighbour-search kernels, descriptor, 3 species-
-    #                          partition kernels, tensor-core networks, 2 energy-reduction
-    #                          kernels, adjoint, force output
+    # types, the neighbour search (one kernel per structure block, which
+    # builds its own cell lists, when the plan takes the per-structure
+    # search: at least twice as many structures as SMs; otherwise binning,
+    # three scan kernels, scatter and the search), descriptor, 3 species-
+    # partition kernels, tensor-core networks, 2 energy-reduction kernels,
+    # adjoint, force output
+    nb_kernel = (tuned or {}).get("neighbour_kernel") or args.neighbour_kernel or "atom"
+    per_struct = nb_kernel in ("struct", "struct_half") and \
+        len(nat) >= 2 * torch.cuda.get_device_properties(local).multi_processor_count
+    launches_per_step = 11 if per_struct else 16
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
