@@ -1700,7 +1700,7 @@ int atomic_eval_fused(const double* coo_i, int type_i, int n_j, const double* co
   // one block is faster for short rows (a cluster's launch and barriers
   // cost a few microseconds), the cluster for long ones
   const bool cluster = g.atom_fused == 3 || (g.atom_fused == 2 && n_j >= AE_ATOM_CLUSTER_ROWS);
-  const int e = ae_launch_atom(g.pd, n_j, g_atom.mdev, g_atom.mdev + in_bytes, cluster,
+  const int e = ae_launch_atom(g.pd, *hd, g_atom.mdev, g_atom.mdev + in_bytes, cluster,
                                g_atom.stream);
   if (e == AE_ATOM_NA) return AE_ATOM_NA;
   if (e || cudaStreamSynchronize(g_atom.stream) != cudaSuccess) return AENET_ERR_CUDA;

@@ -291,8 +291,9 @@ int ae_launch_stale_order(int natoms, const StructGeom* geom, const int* atom_st
 int ae_launch_chebyshev_forward(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);
 // One FP64 Chebyshev atom per launch (the per-atom entry points): one
-// block, or (cluster != 0) a cluster of eight blocks; inputs and outputs in
-// mapped host memory.  Input: AtomCallHeader, then at
+// block, or (cluster != 0) a cluster of eight blocks; the header comes as
+// a launch argument, rows and outputs in mapped host memory.  Input: the
+// header (also kept at the start of the block), then at
 // AE_ATOM_IN_VEC the neighbour vectors (R_ij, |R_ij|) as double4[n] and
 // their species (0-based) as int[n].  Output: E_i (double), status
 // (unsigned), then at AE_ATOM_OUT_F the forces double[n + 1][3] (central
@@ -310,8 +311,8 @@ struct AtomCallHeader {
 #define AE_ATOM_NMAX 512
 #define AE_ATOM_NA (-2)
 #define AE_ATOM_CLUSTER_ROWS 96   // rows from which the fused per-atom call takes the cluster
-int ae_launch_atom(const PotDevice& pd, int n, const void* in, void* out, int cluster,
-                   cudaStream_t s);
+int ae_launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, void* out,
+                   int cluster, cudaStream_t s);
 int ae_launch_chebyshev_adjoint(const PotDevice& pd, const DescBuffers& b,
                                 int fp64, cudaStream_t s);
 int ae_launch_chebyshev_tangent(const PotDevice& pd, const DescBuffers& b,

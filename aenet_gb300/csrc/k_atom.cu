@@ -26,9 +26,10 @@
 // angular records, their partial descriptor sums and their partial pair
 // gradients through distributed shared memory between cluster barriers,
 // and every block runs the (small) network itself.  Every sum runs in a
-// fixed order, so repeated calls give identical bits.  The call's inputs
-// are read from, and its outputs written to, mapped pinned host memory: a
-// call is one launch and one stream synchronisation.
+// fixed order, so repeated calls give identical bits.  The call's row is
+// read from, and its outputs written to, mapped pinned host memory (the
+// row length, species and forces flag come as launch arguments): a call is
+// one launch and one stream synchronisation.
 #include <cooperative_groups.h>
 
 #include "common.h"
@@ -487,11 +488,11 @@ struct AtomSmem {
 
 template <int RB, int AB>
 __global__ void __launch_bounds__(AT_THREADS, 1)
-    k_atom(PotDevice pd, const unsigned char* __restrict__ in, unsigned char* __restrict__ out) {
+    k_atom(PotDevice pd, AtomCallHeader hd, const unsigned char* __restrict__ in,
+           unsigned char* __restrict__ out) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   __shared__ int s_wcnt[AT_WARPS];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const AtomCallHeader hd = *reinterpret_cast<const AtomCallHeader*>(in);
   const int n = hd.n, ti = hd.ti;
   const double4_32a* __restrict__ vin = reinterpret_cast<const double4_32a*>(in + AE_ATOM_IN_VEC);
   const int* __restrict__ tin =
@@ -543,7 +544,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1)
 
 template <int RB, int AB>
 __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
-    k_atom_cluster(PotDevice pd, const unsigned char* __restrict__ in,
+    k_atom_cluster(PotDevice pd, AtomCallHeader hd, const unsigned char* __restrict__ in,
                    unsigned char* __restrict__ out) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   __shared__ int s_wcnt[AT_WARPS];
@@ -551,7 +552,6 @@ __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const AtomCallHeader hd = *reinterpret_cast<const AtomCallHeader*>(in);
   const int n = hd.n, ti = hd.ti;
   const double4_32a* __restrict__ vin = reinterpret_cast<const double4_32a*>(in + AE_ATOM_IN_VEC);
   const int* __restrict__ tin =
@@ -649,9 +649,9 @@ __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
 }
 
 template <int RB, int AB>
-int launch_atom(const PotDevice& pd, int n, const void* in, void* out, bool cluster,
-                cudaStream_t s) {
-  const size_t smem = at_smem_bytes<RB, AB>(n, pd.nsf_pad, cluster);
+int launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, void* out,
+                bool cluster, cudaStream_t s) {
+  const size_t smem = at_smem_bytes<RB, AB>(hd.n, pd.nsf_pad, cluster);
   if (smem > 200 * 1024) return AE_ATOM_NA;
   const unsigned char* pin = static_cast<const unsigned char*>(in);
   unsigned char* pout = static_cast<unsigned char*>(out);
@@ -665,7 +665,7 @@ int launch_atom(const PotDevice& pd, int n, const void* in, void* out, bool clus
       if (e != cudaSuccess) return (int)e;
       opted = true;
     }
-    k_atom_cluster<RB, AB><<<AC_CTAS, AT_THREADS, smem, s>>>(pd, pin, pout);
+    k_atom_cluster<RB, AB><<<AC_CTAS, AT_THREADS, smem, s>>>(pd, hd, pin, pout);
   } else {
     static bool opted = false;
     if (!opted) {
@@ -674,16 +674,16 @@ int launch_atom(const PotDevice& pd, int n, const void* in, void* out, bool clus
       if (e != cudaSuccess) return (int)e;
       opted = true;
     }
-    k_atom<RB, AB><<<1, AT_THREADS, smem, s>>>(pd, pin, pout);
+    k_atom<RB, AB><<<1, AT_THREADS, smem, s>>>(pd, hd, pin, pout);
   }
   return (int)cudaGetLastError();
 }
 
 }  // namespace
 
-int ae_launch_atom(const PotDevice& pd, int n, const void* in, void* out, int cluster,
-                   cudaStream_t s) {
-  if (n < 0 || n > AE_ATOM_NMAX) return AE_ATOM_NA;
+int ae_launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, void* out,
+                   int cluster, cudaStream_t s) {
+  if (hd.n < 0 || hd.n > AE_ATOM_NMAX) return AE_ATOM_NA;
   int rN = 0, aN = 0;
   for (int t = 0; t < pd.ntypes; ++t) {
     if (pd.sp[t].sftype != AE_SF_CHEBYSHEV) return AE_ATOM_NA;
@@ -692,7 +692,7 @@ int ae_launch_atom(const PotDevice& pd, int n, const void* in, void* out, int cl
     for (int l = 1; l < pd.sp[t].net.nlayers; ++l)
       if (pd.sp[t].net.nnodes[l] > AE_MAXNODES) return AE_ATOM_NA;
   }
-  if (rN <= 17 && aN <= 9) return launch_atom<17, 9>(pd, n, in, out, cluster != 0, s);
-  if (rN <= 24 && aN <= 16) return launch_atom<24, 16>(pd, n, in, out, cluster != 0, s);
+  if (rN <= 17 && aN <= 9) return launch_atom<17, 9>(pd, hd, in, out, cluster != 0, s);
+  if (rN <= 24 && aN <= 16) return launch_atom<24, 16>(pd, hd, in, out, cluster != 0, s);
   return AE_ATOM_NA;
 }
