@@ -10,13 +10,15 @@
 //            cut-off and unit vector (the per-neighbour values of sfb_eval,
 //            src/ext/sfbasis.f90:488-512); angular neighbours compacted in
 //            list order;
-//   forward  warp 0 over the neighbours (radial T_n, chebyshev.f90:41-128),
+//   forward  warps 0-2 over the neighbours (radial T_n, chebyshev.f90:41-128),
 //            the other warps over the pairs j < k of angular neighbours;
 //            the per-thread sums are reduced column by column through
 //            shared memory, four lanes per feature;
-//   network  eight lanes per node, forward and back (ff_eval / ff_deriv,
+//   network  eight lanes per node for the sums, one lane per node for the
+//            activations, forward and back (ff_eval / ff_deriv,
 //            src/ext/feedforward.f90:586-757);
-//   adjoint  thread per neighbour (radial) and per pair (angular); the
+//   adjoint  thread per neighbour (radial, warps 0-2) and per pair
+//            (angular, warps 3-7, at the same time); the
 //            pair gradients of each round are gathered per neighbour in a
 //            fixed order; the central atom takes minus the sum of the
 //            neighbour forces (aenet.f90:471-477).
@@ -49,12 +51,19 @@ using cheb::SFB_PI;
 
 constexpr int AT_THREADS = 256;
 constexpr int AT_WARPS = AT_THREADS / 32;
-constexpr int AT_RAD = 32;                    // radial threads (warp 0)
-constexpr int AT_ANG = AT_THREADS - AT_RAD;   // pair threads (warps 1 ..)
+// FP64 runs at 2 lanes per clock per SM, so every phase spreads its FP64
+// work over as many warps as it can: radial terms on warps 0-2, pairs on
+// warps 3-7 (forward and adjoint at the same time), radial and angular
+// cut-offs of a row on two threads, activations on one warp
+constexpr int AT_RAD = 96;                    // radial threads (warps 0-2)
+constexpr int AT_ANG = AT_THREADS - AT_RAD;   // pair threads (warps 3-7)
+constexpr int AT_HALF = AT_THREADS / 2;       // rows per staging pass
 constexpr int AT_LPN = 8;                     // lanes per network node
 constexpr int AT_LPF = 4;                     // lanes per feature sum
 constexpr int AT_NSTRIDE = AE_MAXNODES + 1;
 constexpr int AC_CTAS = 8;                    // blocks of the cluster form
+constexpr int AT_WMAX = 4096;                 // network weights staged in shared memory
+                                              // (doubles; larger networks read L2)
 
 template <int RB, int AB>
 __host__ __device__ constexpr size_t at_red_elems() {
@@ -67,12 +76,19 @@ __host__ __device__ constexpr size_t at_red_elems() {
 // the row -> angular index map; forces, angular gradients, reduction and
 // network scratch
 template <int RB, int AB>
-__host__ __device__ size_t at_smem_bytes(int n, int nsf_pad, bool cluster) {
+__host__ __device__ size_t at_smem_bytes(int n, int nsf_pad, bool cluster, int wcount) {
   return (cluster ? 6 : 4) * sizeof(double4_32a) * (size_t)n + 6 * sizeof(double) * (size_t)n +
          (cluster ? 4 * (size_t)n : 0) +
          sizeof(double) * (at_red_elems<RB, AB>() + 3 * (size_t)nsf_pad +
-                           2 * (size_t)AE_MAXLAYERS * AT_NSTRIDE + 4) +
+                           2 * (size_t)AE_MAXLAYERS * AT_NSTRIDE + 4 + (size_t)wcount) +
          64;
+}
+
+// first and one-past-last weight of species t's network in the weight array
+__host__ __device__ inline void net_range(const NetTable& net, int& w0, int& w1) {
+  const int L = net.nlayers;
+  w0 = net.w_off[0];
+  w1 = net.w_off[L - 2] + net.pitch[L - 2] * net.nnodes[L - 1];
 }
 
 __device__ __forceinline__ int tri_index(int a, int b, int na) {
@@ -100,15 +116,18 @@ struct AtomCtx {
 
 // Rows [j0, j1) of the call: sv/sr at j - j0, the angular ones compacted in
 // row order into au/af (slot = the row's index j), amap[j - j0] = the
-// compacted index or -1 (when amap is given).  Block-wide; returns the
-// number of angular rows.
+// compacted index or -1 (when amap is given).  AT_HALF rows per pass: the
+// first half of the block computes their radial records, the second half
+// their angular ones.  Block-wide; returns the number of angular rows.
 __device__ int stage_rows(const AtomCtx& c, const ChebTable& ct, const double4_32a* vin,
                           const int* tin, int j0, int j1, double4_32a* sv, double4_32a* sr,
                           double4_32a* au, double4_32a* af, int* amap, int* s_wcnt) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool ang_half = tid >= AT_HALF;
+  const int h = ang_half ? tid - AT_HALF : tid;
   int na = 0;
-  for (int c0 = j0; c0 < j1; c0 += AT_THREADS) {
-    const int j = c0 + tid;
+  for (int c0 = j0; c0 < j1; c0 += AT_HALF) {
+    const int j = c0 + h;
     bool inA = false;
     double4_32a v;
     v.x = v.y = v.z = v.w = 0.0;
@@ -116,25 +135,29 @@ __device__ int stage_rows(const AtomCtx& c, const ChebTable& ct, const double4_3
     if (j < j1) {
       v = vin[j];
       const int t = tin[j];
-      sv[j - j0] = v;
-      const double d = v.w;
       s = c.multi ? (double)ct.spin[t] : 0.0;
-      double4_32a r;
-      r.x = r.y = r.z = 0.0;
-      r.w = s;
-      if (d <= c.r_Rc && d > SFB_EPS) {
-        cutoff_a(d, c.r_Rc, c.r_a, r.y, r.z);
-        r.x = radial_x(d, c.r_Rc, c.two_over_rc);
+      const double d = v.w;
+      if (!ang_half) {
+        sv[j - j0] = v;
+        double4_32a r;
+        r.x = r.y = r.z = 0.0;
+        r.w = s;
+        if (d <= c.r_Rc && d > SFB_EPS) {
+          cutoff_a(d, c.r_Rc, c.r_a, r.y, r.z);
+          r.x = radial_x(d, c.r_Rc, c.two_over_rc);
+        }
+        sr[j - j0] = r;
+      } else {
+        inA = d <= c.a_Rc && d >= SFB_EPS;
       }
-      sr[j - j0] = r;
-      inA = d <= c.a_Rc && d >= SFB_EPS;
     }
+    // compaction over the angular half's warps
     const unsigned m = __ballot_sync(0xffffffffu, inA);
-    if (lane == 0) s_wcnt[warp] = __popc(m);
+    if (ang_half && lane == 0) s_wcnt[warp - AT_HALF / 32] = __popc(m);
     __syncthreads();
     int off = na, tot = 0;
-    for (int w = 0; w < AT_WARPS; ++w) {
-      if (w < warp) off += s_wcnt[w];
+    for (int w = 0; w < AT_HALF / 32; ++w) {
+      if (w < warp - AT_HALF / 32) off += s_wcnt[w];
       tot += s_wcnt[w];
     }
     const int k = off + __popc(m & ((1u << lane) - 1u));
@@ -151,9 +174,9 @@ __device__ int stage_rows(const AtomCtx& c, const ChebTable& ct, const double4_3
       au[k] = u;
       af[k] = f;
     }
-    if (amap && j < j1) amap[j - j0] = inA ? k : -1;
+    if (ang_half && amap && j < j1) amap[j - j0] = inA ? k : -1;
     na += tot;
-    __syncthreads();   // s_wcnt is rewritten by the next chunk
+    __syncthreads();   // s_wcnt is rewritten by the next pass
   }
   return na;
 }
@@ -166,15 +189,15 @@ __device__ void forward_sums(const AtomCtx& c, const ChebTable& ct, const double
                              const double4_32a* sr, int nl, const double4_32a* au,
                              const double4_32a* af, int na, int p_lo, int p_hi, double* red,
                              double* fsum) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   double* red_r = red;                       // [2 RB][AT_RAD]
   double* red_a = red + 2 * RB * AT_RAD;     // [2 AB][AT_ANG]
   const int rN = c.rN, aN = c.aN;
-  if (warp == 0) {
+  if (tid < AT_RAD) {
     double acc[RB], accs[RB];
 #pragma unroll
     for (int q = 0; q < RB; ++q) acc[q] = accs[q] = 0.0;
-    for (int j = lane; j < nl; j += AT_RAD) {
+    for (int j = tid; j < nl; j += AT_RAD) {
       const double d = sv[j].w;
       if (d <= c.r_Rc && d > SFB_EPS) {
         const double4_32a r = sr[j];
@@ -196,8 +219,8 @@ __device__ void forward_sums(const AtomCtx& c, const ChebTable& ct, const double
     }
 #pragma unroll
     for (int q = 0; q < RB; ++q) {
-      red_r[q * AT_RAD + lane] = acc[q];
-      red_r[(RB + q) * AT_RAD + lane] = accs[q];
+      red_r[q * AT_RAD + tid] = acc[q];
+      red_r[(RB + q) * AT_RAD + tid] = accs[q];
     }
   } else {
     const int p0 = tid - AT_RAD;
@@ -268,14 +291,19 @@ __device__ void forward_sums(const AtomCtx& c, const ChebTable& ct, const double
 // node y and leaves dE/dG of the raw descriptor (times E_scale and the
 // normalisation scale) in D.  Block-wide.
 __device__ double atom_network(const PotDevice& pd, const SpeciesTable& sp, int ti,
-                               const double* G, double* D, double* act, double* der) {
+                               const double* G, double* D, double* act, double* der,
+                               const double* wsm) {
   const int tid = threadIdx.x;
   const NetTable& net = sp.net;
   const int L = net.nlayers;
-  const double* __restrict__ W = pd.w64;
+  // the species' weights: staged in shared memory (wsm, from its first
+  // weight on) or read from the global table
+  int w0, w1;
+  net_range(net, w0, w1);
+  auto layer = [&](int l) { return wsm ? wsm + (net.w_off[l] - w0) : pd.w64 + net.w_off[l]; };
   for (int l = 0; l < L - 1; ++l) {
     const int nin = net.nnodes[l], nout = net.nnodes[l + 1];
-    const double* Wl = W + net.w_off[l];
+    const double* Wl = layer(l);
     const int pitch = net.pitch[l];
     const double* hin = (l == 0) ? G : act + l * AT_NSTRIDE;
     double* hout = act + (l + 1) * AT_NSTRIDE;
@@ -291,12 +319,15 @@ __device__ double atom_network(const PotDevice& pd, const SpeciesTable& sp, int 
       part += __shfl_xor_sync(0xffffffffu, part, 4);
       part += __shfl_xor_sync(0xffffffffu, part, 2);
       part += __shfl_xor_sync(0xffffffffu, part, 1);
-      if (o < nout && sub == 0) {
-        double y, dy;
-        activate<double>(fa, part + Wl[(size_t)o * pitch + nin], y, dy);
-        hout[o] = y;
-        dout[o] = dy;
-      }
+      if (o < nout && sub == 0) hout[o] = part + Wl[(size_t)o * pitch + nin];
+    }
+    __syncthreads();
+    // the activations on the first warp(s), one node per lane
+    for (int o = tid; o < nout; o += AT_THREADS) {
+      double y, dy;
+      activate<double>(fa, hout[o], y, dy);
+      hout[o] = y;
+      dout[o] = dy;
     }
     __syncthreads();
   }
@@ -305,7 +336,7 @@ __device__ double atom_network(const PotDevice& pd, const SpeciesTable& sp, int 
   const double* delta = der + (L - 1) * AT_NSTRIDE;
   for (int l = L - 2; l >= 0; --l) {
     const int nin = net.nnodes[l], nout = net.nnodes[l + 1];
-    const double* Wl = W + net.w_off[l];
+    const double* Wl = layer(l);
     const int pitch = net.pitch[l];
     double* dl = (l == 0) ? D : der + l * AT_NSTRIDE;
     for (int kb = 0; kb < nin; kb += AT_THREADS / AT_LPN) {
@@ -327,56 +358,57 @@ __device__ double atom_network(const PotDevice& pd, const SpeciesTable& sp, int 
   return y;
 }
 
-// Radial part of the force on rows [0, nl): -c R_ij / d into sF.
-template <int RB>
-__device__ void adjoint_radial(const AtomCtx& c, const ChebTable& ct, const double* D,
-                               const double4_32a* sv, const double4_32a* sr, int nl, double* sF) {
-  const int rN = c.rN;
-  double gr[RB], grs[RB];
+// The adjoint: radial part of the force on rows [0, nl) (-c R_ij / d into
+// sF) on warps 0-2 while warps 3-7 take the gradients of the pairs
+// [p_lo, p_hi) on both partners, in rounds of AT_ANG pairs through pbuf,
+// gathered per angular neighbour in a fixed order into aF[3 a] (zeroed
+// here).  Block-wide.
+template <int RB, int AB>
+__device__ void adjoint_rows_pairs(const AtomCtx& c, const ChebTable& ct, const double* D,
+                                   const double4_32a* sv, const double4_32a* sr, int nl,
+                                   double* sF, const double4_32a* au, const double4_32a* af,
+                                   int na, int p_lo, int p_hi, double* pbuf, double* aF) {
+  const int tid = threadIdx.x, rN = c.rN, aN = c.aN;
+  for (int a = tid; a < na; a += AT_THREADS) aF[3 * a] = aF[3 * a + 1] = aF[3 * a + 2] = 0.0;
+  __syncthreads();
+  if (tid < AT_RAD) {
+    double gr[RB], grs[RB];
 #pragma unroll
-  for (int q = 0; q < RB; ++q) {
-    gr[q] = q < rN ? D[ct.r_i1 + q] : 0.0;
-    grs[q] = (c.multi && q < rN) ? D[ct.r_i2 + q] : 0.0;
-  }
-  for (int j = threadIdx.x; j < nl; j += AT_THREADS) {
-    const double4_32a v = sv[j];
-    const double d = v.w;
-    double cc = 0.0;
-    if (d <= c.r_Rc && d > SFB_EPS) {
-      const double4_32a r = sr[j];
-      const double fc = r.y, dfc = r.z, s = r.w, x = r.x, x2 = x + x;
-      double tm1 = 1.0, t0 = x, um1 = 1.0, u0 = x2;
-      cc = (gr[0] + s * grs[0]) * dfc;
+    for (int q = 0; q < RB; ++q) {
+      gr[q] = q < rN ? D[ct.r_i1 + q] : 0.0;
+      grs[q] = (c.multi && q < rN) ? D[ct.r_i2 + q] : 0.0;
+    }
+    for (int j = tid; j < nl; j += AT_RAD) {
+      const double4_32a v = sv[j];
+      const double d = v.w;
+      double cc = 0.0;
+      if (d <= c.r_Rc && d > SFB_EPS) {
+        const double4_32a r = sr[j];
+        const double fc = r.y, dfc = r.z, s = r.w, x = r.x, x2 = x + x;
+        double tm1 = 1.0, t0 = x, um1 = 1.0, u0 = x2;
+        cc = (gr[0] + s * grs[0]) * dfc;
 #pragma unroll
-      for (int q = 1; q < RB; ++q) {
-        if (q < rN) {
-          const double gq = gr[q] + s * grs[q];
-          const double dT = (double)q * um1 * c.two_over_rc;
-          cc = fma(gq, fma(dfc, t0, fc * dT), cc);
-          const double tn = fma(x2, t0, -tm1);
-          tm1 = t0;
-          t0 = tn;
-          const double un = fma(x2, u0, -um1);
-          um1 = u0;
-          u0 = un;
+        for (int q = 1; q < RB; ++q) {
+          if (q < rN) {
+            const double gq = gr[q] + s * grs[q];
+            const double dT = (double)q * um1 * c.two_over_rc;
+            cc = fma(gq, fma(dfc, t0, fc * dT), cc);
+            const double tn = fma(x2, t0, -tm1);
+            tm1 = t0;
+            t0 = tn;
+            const double un = fma(x2, u0, -um1);
+            um1 = u0;
+            u0 = un;
+          }
         }
       }
+      const double inv = (d > SFB_EPS && d < 1e29) ? cc / d : 0.0;
+      sF[3 * j] = -(inv * v.x);
+      sF[3 * j + 1] = -(inv * v.y);
+      sF[3 * j + 2] = -(inv * v.z);
     }
-    const double inv = (d > SFB_EPS && d < 1e29) ? cc / d : 0.0;
-    sF[3 * j] = -(inv * v.x);
-    sF[3 * j + 1] = -(inv * v.y);
-    sF[3 * j + 2] = -(inv * v.z);
   }
-}
-
-// Gradients of the pairs [p_lo, p_hi) on both partners, in rounds of
-// AT_THREADS pairs through pbuf, gathered per angular neighbour in a fixed
-// order and added to aF[3 a] (zeroed by the caller).  Block-wide.
-template <int AB>
-__device__ void adjoint_pairs(const AtomCtx& c, const ChebTable& ct, const double* D,
-                              const double4_32a* au, const double4_32a* af, int na, int p_lo,
-                              int p_hi, double* pbuf, double* aF) {
-  const int tid = threadIdx.x, aN = c.aN;
+  const int pt = tid - AT_RAD;   // pair thread
   double gav[AB], gasv[AB];
 #pragma unroll
   for (int q = 0; q < AB; ++q) {
@@ -384,51 +416,52 @@ __device__ void adjoint_pairs(const AtomCtx& c, const ChebTable& ct, const doubl
     gasv[q] = (c.multi && q < aN) ? D[ct.a_i2 + q] : 0.0;
   }
   PairWalk pw;
-  if (p_lo + tid < p_hi) pw.start(p_lo + tid, na);
-  for (int P0 = p_lo; P0 < p_hi; P0 += AT_THREADS) {
-    __syncthreads();   // the previous round's gather is done with pbuf
-    const int p = P0 + tid;
-    double g6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    if (p < p_hi) {
-      const double4_32a ua = au[pw.a], uk = au[pw.b], fa = af[pw.a], fk = af[pw.b];
-      const double cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
-      const double w = fa.x * fk.x;
-      const double ss = fa.z * fk.z;
-      double x, dxdc;
-      angular_arg(cosv, c.legacy, x, dxdc);
-      const double x2 = x + x;
-      double tm1 = 1.0, t0 = x, um1 = 1.0, u0 = x2;
-      double Av = fma(ss, gasv[0], gav[0]), Bv = 0.0;
+  if (pt >= 0 && p_lo + pt < p_hi) pw.start(p_lo + pt, na);
+  for (int P0 = p_lo; P0 < p_hi; P0 += AT_ANG) {
+    const int p = P0 + pt;
+    if (pt >= 0) {
+      double g6[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      if (p < p_hi) {
+        const double4_32a ua = au[pw.a], uk = au[pw.b], fa = af[pw.a], fk = af[pw.b];
+        const double cosv = ua.x * uk.x + ua.y * uk.y + ua.z * uk.z;
+        const double w = fa.x * fk.x;
+        const double ss = fa.z * fk.z;
+        double x, dxdc;
+        angular_arg(cosv, c.legacy, x, dxdc);
+        const double x2 = x + x;
+        double tm1 = 1.0, t0 = x, um1 = 1.0, u0 = x2;
+        double Av = fma(ss, gasv[0], gav[0]), Bv = 0.0;
 #pragma unroll
-      for (int q = 1; q < AB; ++q) {
-        if (q < aN) {
-          const double cq = fma(ss, gasv[q], gav[q]);
-          Av = fma(cq, t0, Av);
-          Bv = fma(cq * (double)q, um1, Bv);
-          const double tn = fma(x2, t0, -tm1);
-          tm1 = t0;
-          t0 = tn;
-          const double un = fma(x2, u0, -um1);
-          um1 = u0;
-          u0 = un;
+        for (int q = 1; q < AB; ++q) {
+          if (q < aN) {
+            const double cq = fma(ss, gasv[q], gav[q]);
+            Av = fma(cq, t0, Av);
+            Bv = fma(cq * (double)q, um1, Bv);
+            const double tn = fma(x2, t0, -tm1);
+            tm1 = t0;
+            t0 = tn;
+            const double un = fma(x2, u0, -um1);
+            um1 = u0;
+            u0 = un;
+          }
         }
+        const double inva = ua.w, invk = uk.w;
+        const double Bc = w * Bv * dxdc;
+        const double dEda = fa.y * fk.x * Av, ca = Bc * inva;
+        const double dEdk = fa.x * fk.y * Av, ck = Bc * invk;
+        g6[0] = dEda * ua.x + ca * (uk.x - cosv * ua.x);
+        g6[1] = dEda * ua.y + ca * (uk.y - cosv * ua.y);
+        g6[2] = dEda * ua.z + ca * (uk.z - cosv * ua.z);
+        g6[3] = dEdk * uk.x + ck * (ua.x - cosv * uk.x);
+        g6[4] = dEdk * uk.y + ck * (ua.y - cosv * uk.y);
+        g6[5] = dEdk * uk.z + ck * (ua.z - cosv * uk.z);
+        pw.advance(na, AT_ANG);
       }
-      const double inva = ua.w, invk = uk.w;
-      const double Bc = w * Bv * dxdc;
-      const double dEda = fa.y * fk.x * Av, ca = Bc * inva;
-      const double dEdk = fa.x * fk.y * Av, ck = Bc * invk;
-      g6[0] = dEda * ua.x + ca * (uk.x - cosv * ua.x);
-      g6[1] = dEda * ua.y + ca * (uk.y - cosv * ua.y);
-      g6[2] = dEda * ua.z + ca * (uk.z - cosv * ua.z);
-      g6[3] = dEdk * uk.x + ck * (ua.x - cosv * uk.x);
-      g6[4] = dEdk * uk.y + ck * (ua.y - cosv * uk.y);
-      g6[5] = dEdk * uk.z + ck * (ua.z - cosv * uk.z);
-      pw.advance(na, AT_THREADS);
-    }
 #pragma unroll
-    for (int q = 0; q < 6; ++q) pbuf[6 * tid + q] = g6[q];
+      for (int q = 0; q < 6; ++q) pbuf[6 * pt + q] = g6[q];
+    }
     __syncthreads();
-    const int P1 = min(p_hi, P0 + AT_THREADS);
+    const int P1 = min(p_hi, P0 + AT_ANG);
     for (int a = tid; a < na; a += AT_THREADS) {
       double gx = aF[3 * a], gy = aF[3 * a + 1], gz = aF[3 * a + 2];
       // pairs (c, a), c < a: the gradient on their second partner
@@ -454,17 +487,28 @@ __device__ void adjoint_pairs(const AtomCtx& c, const ChebTable& ct, const doubl
       aF[3 * a + 1] = gy;
       aF[3 * a + 2] = gz;
     }
+    __syncthreads();   // pbuf is rewritten by the next round
   }
   __syncthreads();
+}
+
+// The species' network weights into shared memory (when there is room for
+// them): issued at the start of the call, so that their loads overlap the
+// row reads; the block's later barriers order them before the network.
+__device__ __forceinline__ void stage_weights(const NetTable& net, const double* W, double* wsm) {
+  if (!wsm) return;
+  int w0, w1;
+  net_range(net, w0, w1);
+  for (int q = threadIdx.x; q < w1 - w0; q += AT_THREADS) wsm[q] = W[w0 + q];
 }
 
 // shared-memory carve-up of a call
 struct AtomSmem {
   double4_32a *sv, *sr, *au, *af, *lau, *laf;
-  double *sF, *aF, *red, *fsum, *G, *D, *act, *der, *cen;
+  double *sF, *aF, *red, *fsum, *G, *D, *act, *der, *cen, *wsm;
   int* amap;
   template <int RB, int AB>
-  __device__ void carve(unsigned char* base, int n, int nsf_pad, bool cluster) {
+  __device__ void carve(unsigned char* base, int n, int nsf_pad, bool cluster, int wcount) {
     double4_32a* p = reinterpret_cast<double4_32a*>(base);
     sv = p;
     sr = sv + n;
@@ -482,13 +526,14 @@ struct AtomSmem {
     act = D + nsf_pad;
     der = act + AE_MAXLAYERS * AT_NSTRIDE;
     cen = der + AE_MAXLAYERS * AT_NSTRIDE;
-    amap = cluster ? reinterpret_cast<int*>(cen + 4) : nullptr;
+    wsm = wcount > 0 ? cen + 4 : nullptr;
+    amap = cluster ? reinterpret_cast<int*>(cen + 4 + wcount) : nullptr;
   }
 };
 
 template <int RB, int AB>
 __global__ void __launch_bounds__(AT_THREADS, 1)
-    k_atom(PotDevice pd, AtomCallHeader hd, const unsigned char* __restrict__ in,
+    k_atom(PotDevice pd, AtomCallHeader hd, int wcount, const unsigned char* __restrict__ in,
            unsigned char* __restrict__ out) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   __shared__ int s_wcnt[AT_WARPS];
@@ -502,7 +547,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1)
   AtomCtx c;
   c.init(ct);
   AtomSmem sm{};
-  sm.carve<RB, AB>(smem_raw, n, pd.nsf_pad, false);
+  sm.carve<RB, AB>(smem_raw, n, pd.nsf_pad, false, wcount);
+  stage_weights(sp.net, pd.w64, sm.wsm);
 
   const int na = stage_rows(c, ct, vin, tin, 0, n, sm.sv, sm.sr, sm.au, sm.af, nullptr, s_wcnt);
   const int np = na * (na - 1) / 2;
@@ -511,16 +557,15 @@ __global__ void __launch_bounds__(AT_THREADS, 1)
   for (int k = tid; k < sp.nsf; k += AT_THREADS)
     sm.G[k] = (sm.fsum[k] - pd.shift[nrow + k]) * pd.scale[nrow + k];
   __syncthreads();
-  const double y = atom_network(pd, sp, ti, sm.G, sm.D, sm.act, sm.der);
+  const double y = atom_network(pd, sp, ti, sm.G, sm.D, sm.act, sm.der, sm.wsm);
   if (tid == 0) {
     *reinterpret_cast<double*>(out) = sp.E_scale * y + sp.E_shift + sp.E_atom;
     *reinterpret_cast<unsigned*>(out + 8) = 0u;
   }
   if (!hd.forces) return;
 
-  adjoint_radial<RB>(c, ct, sm.D, sm.sv, sm.sr, n, sm.sF);
-  for (int a = tid; a < na; a += AT_THREADS) sm.aF[3 * a] = sm.aF[3 * a + 1] = sm.aF[3 * a + 2] = 0.0;
-  adjoint_pairs<AB>(c, ct, sm.D, sm.au, sm.af, na, 0, np, sm.red, sm.aF);
+  adjoint_rows_pairs<RB, AB>(c, ct, sm.D, sm.sv, sm.sr, n, sm.sF, sm.au, sm.af, na, 0, np, sm.red,
+                             sm.aF);
   for (int a = tid; a < na; a += AT_THREADS) {
     const int slot = (int)sm.af[a].w;
     sm.sF[3 * slot] -= sm.aF[3 * a];
@@ -544,8 +589,8 @@ __global__ void __launch_bounds__(AT_THREADS, 1)
 
 template <int RB, int AB>
 __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
-    k_atom_cluster(PotDevice pd, AtomCallHeader hd, const unsigned char* __restrict__ in,
-                   unsigned char* __restrict__ out) {
+    k_atom_cluster(PotDevice pd, AtomCallHeader hd, int wcount,
+                   const unsigned char* __restrict__ in, unsigned char* __restrict__ out) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   __shared__ int s_wcnt[AT_WARPS];
   __shared__ int s_na;
@@ -561,7 +606,8 @@ __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
   AtomCtx c;
   c.init(ct);
   AtomSmem sm{};
-  sm.carve<RB, AB>(smem_raw, n, pd.nsf_pad, true);
+  sm.carve<RB, AB>(smem_raw, n, pd.nsf_pad, true, wcount);
+  stage_weights(sp.net, pd.w64, sm.wsm);
   // this block's rows
   const int j0 = (int)((long long)n * rank / AC_CTAS);
   const int j1 = (int)((long long)n * (rank + 1) / AC_CTAS);
@@ -599,16 +645,15 @@ __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
     sm.G[k] = (s - pd.shift[nrow + k]) * pd.scale[nrow + k];
   }
   cl.sync();   // no block reads another's partial sums after this
-  const double y = atom_network(pd, sp, ti, sm.G, sm.D, sm.act, sm.der);
+  const double y = atom_network(pd, sp, ti, sm.G, sm.D, sm.act, sm.der, sm.wsm);
   if (rank == 0 && tid == 0) {
     *reinterpret_cast<double*>(out) = sp.E_scale * y + sp.E_shift + sp.E_atom;
     *reinterpret_cast<unsigned*>(out + 8) = 0u;
   }
   if (!hd.forces) return;
 
-  adjoint_radial<RB>(c, ct, sm.D, sm.sv, sm.sr, nl, sm.sF);
-  for (int a = tid; a < na; a += AT_THREADS) sm.aF[3 * a] = sm.aF[3 * a + 1] = sm.aF[3 * a + 2] = 0.0;
-  adjoint_pairs<AB>(c, ct, sm.D, sm.au, sm.af, na, p_lo, p_hi, sm.red, sm.aF);
+  adjoint_rows_pairs<RB, AB>(c, ct, sm.D, sm.sv, sm.sr, nl, sm.sF, sm.au, sm.af, na, p_lo, p_hi,
+                             sm.red, sm.aF);
   cl.sync();
   // this block's rows: radial part minus every block's angular gradients
   double* Fo = reinterpret_cast<double*>(out + AE_ATOM_OUT_F);
@@ -651,7 +696,20 @@ __global__ void __cluster_dims__(AC_CTAS, 1, 1) __launch_bounds__(AT_THREADS, 1)
 template <int RB, int AB>
 int launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, void* out,
                 bool cluster, cudaStream_t s) {
-  const size_t smem = at_smem_bytes<RB, AB>(hd.n, pd.nsf_pad, cluster);
+  // room for the largest species' weights, unless some network exceeds
+  // AT_WMAX (then every call reads them from L2)
+  int wcount = 0;
+  for (int t = 0; t < pd.ntypes; ++t) {
+    int w0, w1;
+    net_range(pd.sp[t].net, w0, w1);
+    wcount = max(wcount, w1 - w0);
+  }
+  if (wcount > AT_WMAX) wcount = 0;
+  size_t smem = at_smem_bytes<RB, AB>(hd.n, pd.nsf_pad, cluster, wcount);
+  if (smem > 200 * 1024 && wcount > 0) {
+    wcount = 0;
+    smem = at_smem_bytes<RB, AB>(hd.n, pd.nsf_pad, cluster, 0);
+  }
   if (smem > 200 * 1024) return AE_ATOM_NA;
   const unsigned char* pin = static_cast<const unsigned char*>(in);
   unsigned char* pout = static_cast<unsigned char*>(out);
@@ -665,7 +723,7 @@ int launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, v
       if (e != cudaSuccess) return (int)e;
       opted = true;
     }
-    k_atom_cluster<RB, AB><<<AC_CTAS, AT_THREADS, smem, s>>>(pd, hd, pin, pout);
+    k_atom_cluster<RB, AB><<<AC_CTAS, AT_THREADS, smem, s>>>(pd, hd, wcount, pin, pout);
   } else {
     static bool opted = false;
     if (!opted) {
@@ -674,7 +732,7 @@ int launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, v
       if (e != cudaSuccess) return (int)e;
       opted = true;
     }
-    k_atom<RB, AB><<<1, AT_THREADS, smem, s>>>(pd, hd, pin, pout);
+    k_atom<RB, AB><<<1, AT_THREADS, smem, s>>>(pd, hd, wcount, pin, pout);
   }
   return (int)cudaGetLastError();
 }
