@@ -167,3 +167,33 @@ def test_every_declared_function_has_ctypes_signature():
     lib = _lib._declare(C.CDLL(_lib.LIB_PATH))
     missing = [n for n in names if getattr(lib, n).argtypes is None]
     assert not missing, missing
+
+
+def test_options_accept_documented_values_only(lib):
+    """aenet_gpu_set_option takes the keys and values include/aenet_gb300.h
+    documents (host state only, no GPU needed) and returns AENET_ERR_INPUT
+    for anything else; the defaults are restored afterwards."""
+    from aenet_gb300.core import AENET_ERR_INPUT
+    ok = {
+        "angular_domain": ["current", "legacy"],
+        "angular_terms": ["moments", "pairs"],
+        "angular_spin": ["own", "stale"],
+        "neighbour_kernel": ["atom", "cell", "stream", "half", "struct", "struct_half"],
+        "networks": ["tensor", "simt"],
+        "per_atom_kernel": ["fused", "cluster", "block", "graph"],
+        "lanes_per_atom": ["8", "16", "32"],
+        "cell_div": ["1", "2", "3"],
+        "z_refine": ["1", "2", "3", "4"],
+    }
+    defaults = {"angular_domain": "current", "angular_terms": "moments", "angular_spin": "own",
+                "neighbour_kernel": "atom", "networks": "tensor", "per_atom_kernel": "fused",
+                "lanes_per_atom": "16", "cell_div": "2", "z_refine": "1"}
+    try:
+        for key, values in ok.items():
+            for v in values:
+                assert lib.aenet_gpu_set_option(key.encode(), v.encode()) == 0, (key, v)
+            assert lib.aenet_gpu_set_option(key.encode(), b"bogus") == AENET_ERR_INPUT, key
+        assert lib.aenet_gpu_set_option(b"no_such_key", b"1") == AENET_ERR_INPUT
+    finally:
+        for key, v in defaults.items():
+            lib.aenet_gpu_set_option(key.encode(), v.encode())
