@@ -41,7 +41,11 @@ _Bool aenet_all_loaded(void);
 double aenet_free_atom_energy(int type_id);
 
 /* src/aenet.h:12-14, src/aenet.f90:359-408 -- energy of one atom from its
- * neighbours (Cartesian coo_j[3*n_j], 1-based type_j). */
+ * neighbours (Cartesian coo_j[3*n_j], 1-based type_j).  FP64 on the GPU;
+ * on Chebyshev potentials one kernel launch per call (the row read from
+ * and the results written to mapped host memory), otherwise the batch
+ * kernels on a one-row table (option "per_atom_kernel",
+ * include/aenet_gb300.h).  Calls are serialised by a library lock. */
 void aenet_atomic_energy(double coo_i[3], int type_i, int n_j,
                          double coo_j[], int type_j[], double* E_i,
                          int* stat);
