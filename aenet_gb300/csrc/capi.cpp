@@ -934,6 +934,7 @@ struct aenet_gpu_plan {
   double* virial = nullptr;
   unsigned* status = nullptr;
   int nchunks = 0;            // energy-reduction chunks over all structures
+  int one_chunk_each = 0;     // every structure has 1 .. AE_ECHUNK atoms
   double2* e_part = nullptr;
   int* chunk_struct = nullptr;  // [nchunks] structure of each energy chunk
   int* order = nullptr;       // atoms grouped by species (tensor-core networks, training)
@@ -1150,6 +1151,9 @@ int plan_alloc(aenet_gpu_plan* P, const double* coords0, const double* lattices)
   P->natoms = (int)natoms;
   P->ncells = cell_off;
   P->nchunks = nchunks;
+  P->one_chunk_each = 1;
+  for (int s = 0; s < P->nstruc; ++s)
+    if (P->natoms_h[s] < 1 || P->natoms_h[s] > AE_ECHUNK) P->one_chunk_each = 0;
   if (P->cap <= 0) {
     int cap = (int)std::ceil(1.5 * dens_max + 32.0);
     P->cap = (cap + 31) & ~31;
@@ -1387,15 +1391,29 @@ NbBuffers nb_buffers(aenet_gpu_plan* P) {
 
 int ck(int e) { return e ? AENET_ERR_CUDA : 0; }
 
+// The types the neighbour search reads: the per-structure searches take
+// the caller's 1-based ids and write the checked 0-based ones themselves;
+// the other searches read the 0-based ids of the type kernel, launched
+// here.  Null on a launch error.
+const int* search_types(aenet_gpu_plan* P, NbBuffers& nb, const int* d_types, cudaStream_t s) {
+  if ((nb.cell_kernel == 4 || nb.cell_kernel == 5) && nb.struct_order) {
+    nb.types0_out = P->types0;
+    nb.ntypes = P->pd->ntypes;
+    return d_types;
+  }
+  if (ae_launch_types(P->natoms, d_types, P->types0, P->pd->ntypes, P->status, s)) return nullptr;
+  return P->types0;
+}
+
 int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s);
 
 // neighbours + descriptors + networks + energies
 int plan_forward(aenet_gpu_plan* P, const double* d_coords, const int* d_types, double* d_E,
                  double* d_E_atoms, cudaStream_t s) {
-  const PotDevice& pd = *P->pd;
-  if (ck(ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s))) return AENET_ERR_CUDA;
   NbBuffers nb = nb_buffers(P);
-  if (ck(ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s))) return AENET_ERR_CUDA;
+  const int* t_in = search_types(P, nb, d_types, s);
+  if (!t_in) return AENET_ERR_CUDA;
+  if (ck(ae_launch_neighbors(P->natoms, d_coords, t_in, nb, P->fp64, s))) return AENET_ERR_CUDA;
   return plan_eval(P, d_E, d_E_atoms, s);
 }
 
@@ -1425,7 +1443,7 @@ int plan_eval(aenet_gpu_plan* P, double* d_E, double* d_E_atoms, cudaStream_t s)
   if (ck(e)) return AENET_ERR_CUDA;
   if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
   if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->chunk_struct,
-                                         P->E_atom, P->e_part, P->E_struct, s)))
+                                         P->E_atom, P->e_part, P->E_struct, P->one_chunk_each, s)))
     return AENET_ERR_CUDA;
   if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
     return AENET_ERR_CUDA;
@@ -2964,7 +2982,7 @@ EXPORT int aenet_gpu_plan_descriptor_loss_gradient(aenet_gpu_plan* P, const int*
   DescBuffers d = desc_buffers(P, nullptr, false);
   if (plan_networks(P, d, s)) return AENET_ERR_CUDA;
   if (ck(ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->chunk_struct,
-                                         P->E_atom, P->e_part, P->E_struct, s)))
+                                         P->E_atom, P->e_part, P->E_struct, P->one_chunk_each, s)))
     return AENET_ERR_CUDA;
   if (d_E && cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s))
     return AENET_ERR_CUDA;
@@ -3061,11 +3079,12 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   for (int q = 0; q < 9; ++q) cudaEventCreate(&ev[q]);
   int e = 0;
   cudaEventRecord(ev[0], s);
-  e |= ae_launch_types(P->natoms, d_types, P->types0, pd.ntypes, P->status, s);
-  cudaEventRecord(ev[1], s);
   NbBuffers nb = nb_buffers(P);
+  const int* t_in = search_types(P, nb, d_types, s);
+  if (!t_in) e = 1;
+  cudaEventRecord(ev[1], s);
   nb.ev_search = ev[8];
-  e |= ae_launch_neighbors(P->natoms, d_coords, P->types0, nb, P->fp64, s);
+  if (t_in) e |= ae_launch_neighbors(P->natoms, d_coords, t_in, nb, P->fp64, s);
   cudaEventRecord(ev[2], s);
   DescBuffers d = desc_buffers(P, nullptr, false);
   if (d.nb_rank)
@@ -3077,7 +3096,7 @@ EXPORT int aenet_gpu_plan_profile(aenet_gpu_plan* P, const double* d_coords, con
   e |= plan_networks(P, d, s);
   cudaEventRecord(ev[4], s);
   e |= ae_launch_energy_reduce_chunked(P->nstruc, P->nchunks, P->geom_d, P->chunk_struct,
-                                       P->E_atom, P->e_part, P->E_struct, s);
+                                       P->E_atom, P->e_part, P->E_struct, P->one_chunk_each, s);
   if (d_E) cudaMemcpyAsync(d_E, P->E_struct, 8 * (size_t)P->nstruc, cudaMemcpyDeviceToDevice, s);
   cudaEventRecord(ev[5], s);
   const size_t tsz = P->fp64 ? 8 : 4;

@@ -234,6 +234,11 @@ struct NbBuffers {
   // shared-memory capacity of one block (atoms, cells); null = unavailable
   const int* struct_order;
   int smem_atoms, smem_cells;
+  // optional, per-structure search only: the search reads the caller's
+  // 1-based type ids and writes the checked 0-based ones here (no separate
+  // type kernel)
+  int* types0_out;
+  int ntypes;
   int cell_kernel;            // 0: warp per atom; warp per home cell with a lane per
                               // home atom (1) or a lane per candidate (2); 3: warp per
                               // atom over the half stencil, each pair written to both rows;
@@ -342,9 +347,11 @@ int ae_launch_types(int natoms, const int* types1, int* types0, int ntypes,
 // per-structure energies: FP64 sums over chunks of AE_ECHUNK atoms (one
 // warp each; chunk_struct[c] = structure of chunk c), then over each
 // structure's chunks, in pairwise order
+// one_chunk_each: every structure has 1 .. AE_ECHUNK atoms (the chunk pass
+// then writes every total and the combining pass is skipped)
 int ae_launch_energy_reduce_chunked(int nstruc, int nchunks, const StructGeom* geom,
                                     const int* chunk_struct, const double* E_atom, double2* part,
-                                    double* E_struct, cudaStream_t s);
+                                    double* E_struct, int one_chunk_each, cudaStream_t s);
 int ae_launch_energy_reduce(int nstruc, const StructGeom* geom,
                             const double* E_atom, double* E_struct,
                             cudaStream_t s);

@@ -304,12 +304,13 @@ int ae_launch_mlp(const PotDevice& pd, const DescBuffers& b, int fp64, cudaStrea
 
 int ae_launch_energy_reduce_chunked(int nstruc, int nchunks, const StructGeom* geom,
                                     const int* chunk_struct, const double* E_atom, double2* part,
-                                    double* E_struct, cudaStream_t s) {
+                                    double* E_struct, int one_chunk_each, cudaStream_t s) {
   if (nstruc <= 0) return 0;
   if (nchunks > 0)
     k_energy_chunks<<<(nchunks + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, chunk_struct, E_atom,
                                                       part, E_struct);
-  k_energy_struct<<<(nstruc + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, part, E_struct);
+  if (!one_chunk_each)
+    k_energy_struct<<<(nstruc + 7) / 8, 256, 0, s>>>(nstruc, nchunks, geom, part, E_struct);
   return (int)cudaGetLastError();
 }
 

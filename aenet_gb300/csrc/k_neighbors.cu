@@ -56,7 +56,8 @@ __device__ __forceinline__ double wrap_coordinate(double s, unsigned* status) {
 // Lattice coordinates of atom i (geometry.f90:697-712), wrapped, the
 // Cartesian position of the wrapped coordinates and the atom's cell: the
 // per-atom arrays s_wrap, r_wrap, r_f32 (species in w) and cell_of are
-// written; returns the cell's index inside its structure.
+// written (and the checked 0-based species when nb.types0_out is set);
+// returns the cell's index inside its structure.
 __device__ __forceinline__ int wrap_bin_atom(int i, const StructGeom* g, const double* __restrict__ pos,
                                              const int* __restrict__ types, const NbBuffers& nb) {
   double r[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
@@ -97,7 +98,16 @@ __device__ __forceinline__ int wrap_bin_atom(int i, const StructGeom* g, const d
     double x = floor(s[v] * (double)nc[v]);
     cc[v] = x < 0.0 ? 0 : (x >= (double)(nc[v] - 1) ? nc[v] - 1 : (int)x);
   }
-  const int t = types[i];
+  int t = types[i];
+  if (nb.types0_out) {
+    // the caller's 1-based type id, checked and stored 0-based
+    t -= 1;
+    if (t < 0 || t >= nb.ntypes) {
+      atomicOr(nb.status, AE_ST_BAD_TYPE);
+      t = 0;
+    }
+    nb.types0_out[i] = t;
+  }
   for (int v = 0; v < 3; ++v) {
     nb.s_wrap[3 * i + v] = s[v];
     nb.r_wrap[3 * i + v] = rw[v];

@@ -611,16 +611,18 @@ def run_gb300(args):
     if rank == 0 and not args.no_md:
         md = run_md(args, local)
 
-    # types, the neighbour search (one kernel per structure block, which
-    # builds its own cell lists, when the plan takes the per-structure
-    # search: at least twice as many structures as SMs; otherwise binning,
-    # three scan kernels, scatter and the search), descriptor, 3 species-
-    # partition kernels, tensor-core networks, 2 energy-reduction kernels,
-    # adjoint, force output
+    # the neighbour search: one kernel per structure block, which checks
+    # the type ids and builds its own cell lists, when the plan takes the
+    # per-structure search (at least twice as many structures as SMs);
+    # otherwise the type check, binning, three scan kernels, scatter and the
+    # search.  Then descriptor, 3 species-partition kernels, tensor-core
+    # networks, the energy reduction (one kernel when every structure fits
+    # one 2,048-atom chunk, else two), adjoint, force output.
     nb_kernel = (tuned or {}).get("neighbour_kernel") or args.neighbour_kernel or "atom"
     per_struct = nb_kernel in ("struct", "struct_half") and \
         len(nat) >= 2 * torch.cuda.get_device_properties(local).multi_processor_count
-    launches_per_step = 11 if per_struct else 16
+    energy_kernels = 1 if int(np.max(nat)) <= 2048 and int(np.min(nat)) >= 1 else 2
+    launches_per_step = (1 if per_struct else 7) + 1 + 3 + 1 + energy_kernels + 1 + 1
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,

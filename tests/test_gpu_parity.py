@@ -948,7 +948,8 @@ def test_per_structure_search_matches_per_atom_search(cuda, oracle, tmp_path):
     warp-per-atom search on 320 small cells: identical (neighbour, image)
     sets per row, in both precisions, on the plain and the refined grid;
     FP64 energies equal to rounding and against the oracle on a sample of
-    cells."""
+    cells; invalid type ids are reported by the searches (which convert
+    the caller's ids themselves)."""
     torch = cuda
     from aenet_gb300 import workloads
     from aenet_gb300.core import FP64, MIXED, set_option
@@ -981,6 +982,17 @@ def test_per_structure_search_matches_per_atom_search(cuda, oracle, tmp_path):
                 s = got["struct"]
                 if prec == FP64 and z == 4:
                     E = s[4].cpu().numpy()
+        # the per-structure searches check the caller's type ids themselves
+        from aenet_gb300.plan import ST_BAD_TYPE
+        for kern in ("struct", "struct_half"):
+            set_option("neighbour_kernel", kern)
+            plan = Plan(nat, cells, pbc, precision=MIXED)
+            t_bad = t.clone()
+            t_bad[3] = 0
+            t_bad[11] = 99
+            plan.run(p, t_bad)
+            assert plan.status() & ST_BAD_TYPE, kern
+            plan.close()
         oracle.load(w.types, paths)
         for k in (0, 7, 160, 319):
             st = w.structures[k]
