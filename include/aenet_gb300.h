@@ -176,7 +176,11 @@ int aenet_gpu_plan_profile(aenet_gpu_plan* plan, const double* d_coords,
  * FP32 roofline of the descriptor kernels. */
 int aenet_gpu_measure_fp32_peak(double* tflops, void* stream);
 
-/* Device status word of the last run: 0, or AENET_GPU_ST_* bits. */
+/* Device status word of a plan: 0, or the AENET_GPU_ST_* bits raised by
+ * its runs since it was created (the word is not cleared between
+ * aenet_gpu_plan_run calls, so one read after several runs covers them
+ * all; create a new plan, or use the host-buffer entry points, which clear
+ * it per call, for a per-run status). */
 #define AENET_GPU_ST_NB_OVERFLOW 1u
 #define AENET_GPU_ST_BAD_COORD 2u
 #define AENET_GPU_ST_BAD_TYPE 4u
