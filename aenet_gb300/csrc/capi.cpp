@@ -1705,6 +1705,8 @@ int atomic_eval_fused(const double* coo_i, int type_i, int n_j, const double* co
   // R_ij = coo_j - coo_i (sfbasis.f90:488) and its length
   double* vec = reinterpret_cast<double*>(h + AE_ATOM_IN_VEC);
   int* ty = reinterpret_cast<int*>(h + AE_ATOM_IN_VEC + 32 * (size_t)n_j);
+  const double a_Rc = g.pd.sp[type_i - 1].cheb.a_Rc;
+  long long na = 0;   // angular neighbours
   for (int j = 0; j < n_j; ++j) {
     double R[3];
     for (int c = 0; c < 3; ++c) R[c] = coo_j[3 * j + c] - coo_i[c];
@@ -1713,11 +1715,17 @@ int atomic_eval_fused(const double* coo_i, int type_i, int n_j, const double* co
     vec[4 * j + 2] = R[2];
     vec[4 * j + 3] = std::sqrt(R[0] * R[0] + R[1] * R[1] + R[2] * R[2]);
     ty[j] = type_j[j] - 1;
+    if (vec[4 * j + 3] <= a_Rc) ++na;
   }
   const char* ho = h + in_bytes;
-  // one block is faster for short rows (a cluster's launch and barriers
-  // cost a few microseconds), the cluster for long ones
-  const bool cluster = g.atom_fused == 3 || (g.atom_fused == 2 && n_j >= AE_ATOM_CLUSTER_ROWS);
+  // one block is as fast for short rows whose pairs fit one round of its
+  // pair threads (a cluster's launch and barriers cost a few
+  // microseconds); the cluster is faster from there (measured on GB300:
+  // 45 vs 53 us at 78 neighbours and 250 pairs, 114 vs 552 us at 300
+  // neighbours)
+  const bool cluster =
+      g.atom_fused == 3 ||
+      (g.atom_fused == 2 && (n_j >= AE_ATOM_CLUSTER_ROWS || na * (na - 1) / 2 > AE_ATOM_BLOCK_PAIRS));
   const int e = ae_launch_atom(g.pd, *hd, g_atom.mdev, g_atom.mdev + in_bytes, cluster,
                                g_atom.stream);
   if (e == AE_ATOM_NA) return AE_ATOM_NA;

@@ -316,6 +316,8 @@ struct AtomCallHeader {
 #define AE_ATOM_NMAX 512
 #define AE_ATOM_NA (-2)
 #define AE_ATOM_CLUSTER_ROWS 96   // rows from which the fused per-atom call takes the cluster
+#define AE_ATOM_BLOCK_PAIRS 160   // angular pairs beyond which it takes the cluster (one
+                                  // round of the one-block form's pair threads)
 int ae_launch_atom(const PotDevice& pd, const AtomCallHeader& hd, const void* in, void* out,
                    int cluster, cudaStream_t s);
 int ae_launch_chebyshev_adjoint(const PotDevice& pd, const DescBuffers& b,

@@ -91,8 +91,8 @@ extern "C" {
  *       one launch evaluates the call, the row read from and the results
  *       written to mapped host memory, on a cluster of eight blocks that
  *       split the rows and pairs (cluster), on one block (block), or on
- *       one block for rows under 96 neighbours and a cluster from there
- *       (fused, the default); or the batch kernels run on a one-row table
+ *       one block for rows under 96 neighbours with at most 160 angular
+ *       pairs and on a cluster otherwise (fused, the default); or the batch kernels run on a one-row table
  *       from a captured graph (graph; also what Behler potentials, stale
  *       spins and longer rows always take).  Same results to FP64
  *       rounding.
